@@ -1,0 +1,576 @@
+// bridge.cu -- C ABI of libfpt_cuda.so (include/fpt_cuda.h).
+//
+// Replaces the Metal device runtime of FPT Metal (src/metal_bridge.mm):
+// same entry points, same argument meaning, same error convention
+// (0 / 1 plus a message, set_error at src/metal_bridge.mm:41-47).  One
+// process-wide CUDA context on the current device, one stream, and device
+// buffers kept between calls and grown on demand; no caller pointer is
+// retained after a call returns.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fpt_kernels.h"
+#include "fpt_scene.h"
+#include "image_io.h"
+#include "bridge_internal.h"
+
+namespace fpt {
+
+// ------------------------------------------------------------------ errors
+void set_error(char *error, size_t error_len, const char *fmt, ...) {
+    if (!error || error_len == 0) return;
+    va_list args;
+    va_start(args, fmt);
+    vsnprintf(error, error_len, fmt, args);
+    va_end(args);
+}
+
+// ------------------------------------------------------------------ context
+Context &ctx() {
+    static Context c;
+    return c;
+}
+
+bool ensure_device(char *error, size_t error_len) {
+    Context &c = ctx();
+    if (c.ready) return true;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        set_error(error, error_len, "CUDA is unavailable on this machine: %s",
+                  e != cudaSuccess ? cudaGetErrorString(e) : "no device");
+        return false;
+    }
+    e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { set_error(error, error_len, "failed to create CUDA stream: %s", cudaGetErrorString(e)); return false; }
+    cudaEventCreate(&c.ev0);
+    cudaEventCreate(&c.ev1);
+    c.ready = true;
+    return true;
+}
+
+bool ensure_buffer(void **ptr, size_t *cap, size_t need, char *error, size_t error_len) {
+    if (*cap >= need && *ptr) return true;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    size_t bytes = std::max<size_t>(need, 256);
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        set_error(error, error_len, "failed to allocate %zu bytes of device memory: %s", bytes, cudaGetErrorString(e));
+        *ptr = nullptr;
+        return false;
+    }
+    *cap = bytes;
+    return true;
+}
+
+bool check(cudaError_t e, const char *what, char *error, size_t error_len) {
+    if (e == cudaSuccess) return true;
+    set_error(error, error_len, "%s failed: %s", what, cudaGetErrorString(e));
+    return false;
+}
+
+// ------------------------------------------------------------------ scene compilation
+static void host_rotate_camera(const float v_in[3], float yaw, float pitch, float out[3]) {
+    // rotateCamera (shaders/Shaders.metal:425-431) in float.
+    float x = v_in[0], y = v_in[1], z = v_in[2];
+    float sp = std::sin(pitch), cp = std::cos(pitch);
+    float y1 = z * sp + y * cp, z1 = z * cp - y * sp;
+    y = y1; z = z1;
+    float sy = std::sin(yaw), cy = std::cos(yaw);
+    out[0] = x * cy + z * sy;
+    out[1] = y;
+    out[2] = -x * sy + z * cy;
+}
+
+uint32_t scene_kind(const FptCudaSceneExt &e) {
+    switch (e.formula) {
+        case FPT_CUDA_FORMULA_MANDELBULB: return e.power == 8.0f ? KIND_BULB8 : KIND_BULB;
+        case FPT_CUDA_FORMULA_MANDELBOX: return KIND_BOX;
+        case FPT_CUDA_FORMULA_MENGER_FOLD: return KIND_MENGER;
+        case FPT_CUDA_FORMULA_BULB_MENGER_HYBRID: return KIND_HYBRID;
+        default: return KIND_GENERIC;
+    }
+}
+
+bool compile_scene(const FptRenderConfig &c, const FptCudaSceneExt *ext_in, DeviceScene &S, char *error, size_t error_len) {
+    static const FptCudaSceneExt none{};
+    const FptCudaSceneExt &e = ext_in ? *ext_in : none;
+    std::memset(&S, 0, sizeof(S));
+    if (e.formula != 0 && e.formula != FPT_CUDA_FORMULA_MANDELBULB && e.formula != FPT_CUDA_FORMULA_MANDELBOX &&
+        e.formula != FPT_CUDA_FORMULA_MENGER_FOLD && e.formula != FPT_CUDA_FORMULA_BULB_MENGER_HYBRID) {
+        set_error(error, error_len, "unsupported extension formula %u", e.formula);
+        return false;
+    }
+    S.sdf_id = c.sdf_id;
+    S.formula = e.formula;
+    S.kind = scene_kind(e);
+    S.width = c.width; S.height = c.height;
+    S.samples = std::min(std::max(c.samples, 1u), 512u);
+    int bounces = std::min(int(c.render[0]), 8);
+    if (c.sdf_bounce_cap > 0u) bounces = std::min(bounces, int(c.sdf_bounce_cap));
+    S.bounces = uint32_t(std::max(bounces, 0));
+    S.russian_roulette = c.sdf_russian_roulette;
+    S.rr_start = c.sdf_rr_start; S.rr_min_prob = c.sdf_rr_min_prob;
+    S.normal_mode = c.sdf_normal_mode;
+    S.ext_normal = e.normal_mode;
+    S.translucent = (e.formula == 0 && (c.sdf_id == FPT_SDF_GLASS_BALL || c.sdf_id == FPT_SDF_README_GLASS ||
+                                        (c.sdf_id == FPT_SDF_PROGRAM && c.program_material[5] > 0.0f))) ? 1u : 0u;
+    std::memcpy(S.render, c.render, sizeof(S.render));
+    std::memcpy(S.cam_pos, c.camera_position, sizeof(S.cam_pos));
+    S.yaw = c.camera_yaw_pitch[0]; S.pitch = c.camera_yaw_pitch[1]; S.roll = c.camera_roll;
+    S.focal = 1.0f / std::tan(c.camera_fov / 2.0f * 3.14159265359f / 180.0f);
+    S.aa_strength = 0.3f / std::max(float(c.width), float(c.height));
+    S.camera_fov = c.camera_fov;
+    S.camera_dof = c.camera_dof;
+    S.focus_distance = c.focus_distance;
+    std::memcpy(S.world, c.world, sizeof(S.world));
+    std::memcpy(S.world_one_color, c.world_one_color, sizeof(S.world_one_color));
+    const float z1[3] = {0.0f, 0.0f, 1.0f};
+    host_rotate_camera(z1, c.world[2] * 3.14159265359f / 180.0f, c.world[3] * 3.14159265359f / 180.0f, S.env_light_dir);
+    S.world_cos_size = std::cos(std::max(c.world[1], 0.0001f));
+    std::memcpy(S.sun, c.sun, sizeof(S.sun));
+    std::memcpy(S.sun_color, c.sun_color, sizeof(S.sun_color));
+    if (e.sun_intensity > 0.0f) {
+        float n = std::sqrt(e.sun_direction[0] * e.sun_direction[0] + e.sun_direction[1] * e.sun_direction[1] +
+                            e.sun_direction[2] * e.sun_direction[2]);
+        if (!(n > 0.0f)) { set_error(error, error_len, "extension sun direction must be non-zero"); return false; }
+        for (int k = 0; k < 3; ++k) S.sun_dir[k] = e.sun_direction[k] / n;
+        S.sun_power = e.sun_intensity;
+    } else {
+        host_rotate_camera(z1, c.sun[1] * 3.14159265359f / 180.0f, c.sun[2] * 3.14159265359f / 180.0f, S.sun_dir);
+        S.sun_power = 0.0f;
+    }
+    std::memcpy(S.background_gradient, c.background_gradient, sizeof(S.background_gradient));
+    std::memcpy(S.post, c.post, sizeof(S.post));
+    std::memcpy(S.set_values, c.set_values, sizeof(S.set_values));
+    std::memcpy(S.vset_values, c.vset_values, sizeof(S.vset_values));
+    S.material_mode = c.material_mode;
+    S.gradient_count = c.gradient_count;
+    S.fractal_style_mode = c.fractal_style_mode;
+    std::memcpy(S.fractal_style, c.fractal_style, sizeof(S.fractal_style));
+    std::memcpy(S.program_material, c.program_material, sizeof(S.program_material));
+    std::memcpy(S.gradient_stops, c.gradient_stops, sizeof(S.gradient_stops));
+    // deMandelbox constants (shaders/Shaders.metal:731-737).
+    {
+        float SC = 2.8f + c.set_values[2], M = 0.25f + c.set_values[3];
+        S.box_ref[0] = S.box_ref[1] = S.box_ref[2] = SC / M;
+        S.box_ref[3] = std::fabs(SC) / M;
+        S.box_ref[4] = std::min(std::max(M, 1.0e-9f), 1.0f);
+        S.box_ref[5] = std::fabs(SC - 1.0f);
+        S.box_ref[6] = std::pow(std::fabs(SC), -9.0f);
+    }
+    // deIFS rotation (shaders/Shaders.metal:473-493, 707-709).
+    {
+        float ax = -51.080209f + c.set_values[2] * 90.0f, ay = c.set_values[3] * 90.0f, az = -29.096322f + c.set_values[4] * 90.0f;
+        const float k = 3.14159265359f / 180.0f;
+        S.ifs_rot[0] = std::sin(ax * k); S.ifs_rot[1] = std::cos(ax * k);
+        S.ifs_rot[2] = std::sin(ay * k); S.ifs_rot[3] = std::cos(ay * k);
+        S.ifs_rot[4] = std::sin(az * k); S.ifs_rot[5] = std::cos(az * k);
+    }
+    {
+        const float *v = c.vset_values;
+        for (int k = 0; k < 3; ++k) { S.global_rot[2 * k] = std::sin(v[123 + k]); S.global_rot[2 * k + 1] = std::cos(v[123 + k]); }
+        bool ident = std::max(c.set_values[0], 1.0f) == 1.0f;
+        for (int k = 120; k <= 128; ++k) ident = ident && v[k] == 0.0f;
+        S.global_identity = ident ? 1u : 0u;
+        float rx = c.set_values[9], ry = c.set_values[10], rz = c.set_values[11];
+        S.mb_rot[0] = std::sin(rz); S.mb_rot[1] = std::cos(rz);
+        S.mb_rot[2] = std::sin(ry); S.mb_rot[3] = std::cos(ry);
+        S.mb_rot[4] = std::sin(rx); S.mb_rot[5] = std::cos(rx);
+    }
+    // Extension formula.
+    S.iterations = e.iterations;
+    S.bailout = e.bailout;
+    S.power = e.power;
+    S.box_scale = e.box_scale;
+    S.box_fixed2 = float(double(e.box_fixed_radius) * double(e.box_fixed_radius));
+    S.box_min2 = float(double(e.box_min_radius) * double(e.box_min_radius));
+    S.box_min_factor = S.box_min2 > 0.0f ? S.box_fixed2 / S.box_min2 : 1.0f;
+    S.box_fold_limit = e.box_fold_limit;
+    S.box_fold_value = e.box_fold_value;
+    S.menger_scale = e.menger_scale;
+    S.hybrid_period = e.hybrid_period;
+    S.ground_plane = e.ground_plane;
+    S.plane_height = e.plane_height;
+    S.rng = e.rng; S.seed = e.seed; S.brdf = e.brdf;
+    S.albedo = e.albedo; S.ggx_alpha = e.ggx_alpha; S.specular_f0 = e.specular_f0; S.plane_albedo = e.plane_albedo;
+    S.fp64_bisection = e.fp64_bisection;
+    S.surrogate = e.surrogate;
+    S.surrogate_margin = e.surrogate_margin;
+    S.surrogate_safety = e.surrogate_safety;
+    if (e.formula == FPT_CUDA_FORMULA_MANDELBOX && !(S.box_min2 > 0.0f)) {
+        set_error(error, error_len, "Mandelbox minimum radius must be positive");
+        return false;
+    }
+    if ((e.formula == FPT_CUDA_FORMULA_MENGER_FOLD || e.formula == FPT_CUDA_FORMULA_BULB_MENGER_HYBRID) && !(e.menger_scale > 1.0f)) {
+        set_error(error, error_len, "Menger fold scale must be greater than 1");
+        return false;
+    }
+    S.hdri_enabled = c.hdri_enabled;
+    S.hdri_width = c.hdri_width;
+    S.hdri_height = c.hdri_height;
+    std::memcpy(S.hdri_lut, c.hdri_lut, sizeof(S.hdri_lut));
+    S.program_count = std::min<uint32_t>(c.sdf_program_count, FPT_SDF_PROGRAM_MAX_OPS);
+    S.shading_count = std::min<uint32_t>(c.sdf_shading_program_count, FPT_SDF_PROGRAM_MAX_OPS);
+    std::memcpy(S.program, c.sdf_program, sizeof(S.program));
+    std::memcpy(S.shading, c.sdf_shading_program, sizeof(S.shading));
+    return true;
+}
+
+// HDRI hydration (src/metal_bridge.mm:2262-2300): 32x16 FP16 box-filtered LUT.
+bool hydrate_hdri(FptRenderConfig &config, char *error, size_t error_len) {
+    config.hdri_width = 0u;
+    config.hdri_height = 0u;
+    std::memset(config.hdri_lut, 0, sizeof(config.hdri_lut));
+    if (config.hdri_enabled == 0u || config.world[0] != 2.0f) return true;
+    const char *path = reinterpret_cast<const char *>(config.hdri_path);
+    if (!path[0]) { set_error(error, error_len, "HDRI world mode requires world.hdri"); return false; }
+    HdrImage img;
+    std::string err;
+    if (!read_radiance_hdr(path, img, err)) { set_error(error, error_len, "%s", err.c_str()); return false; }
+    config.hdri_width = FPT_HDRI_LUT_WIDTH;
+    config.hdri_height = FPT_HDRI_LUT_HEIGHT;
+    for (uint32_t y = 0; y < FPT_HDRI_LUT_HEIGHT; ++y) {
+        uint32_t sy0 = uint32_t((uint64_t(y) * img.height) / FPT_HDRI_LUT_HEIGHT);
+        uint32_t sy1 = std::max(sy0 + 1u, uint32_t((uint64_t(y + 1u) * img.height) / FPT_HDRI_LUT_HEIGHT));
+        for (uint32_t x = 0; x < FPT_HDRI_LUT_WIDTH; ++x) {
+            uint32_t sx0 = uint32_t((uint64_t(x) * img.width) / FPT_HDRI_LUT_WIDTH);
+            uint32_t sx1 = std::max(sx0 + 1u, uint32_t((uint64_t(x + 1u) * img.width) / FPT_HDRI_LUT_WIDTH));
+            float sum[3] = {0, 0, 0};
+            uint32_t n = 0;
+            for (uint32_t sy = sy0; sy < std::min(sy1, img.height); ++sy)
+                for (uint32_t sx = sx0; sx < std::min(sx1, img.width); ++sx) {
+                    size_t s = (size_t(sy) * img.width + sx) * 3;
+                    sum[0] += img.rgb[s]; sum[1] += img.rgb[s + 1]; sum[2] += img.rgb[s + 2];
+                    ++n;
+                }
+            size_t d = (size_t(y) * FPT_HDRI_LUT_WIDTH + x) * 3;
+            for (int k = 0; k < 3; ++k) config.hdri_lut[d + k] = reference_float_to_half(sum[k] / float(std::max(n, 1u)));
+        }
+    }
+    return true;
+}
+
+// Uploads the scene block (and the extension sky texture) to the device.
+bool upload_scene(DeviceScene &S, const FptCudaSceneExt *ext, char *error, size_t error_len) {
+    Context &c = ctx();
+    if (ext && ext->sky_width > 0) {
+        if (!ext->sky_rgb || ext->sky_height == 0) { set_error(error, error_len, "extension sky needs sky_rgb and sky_height"); return false; }
+        size_t bytes = size_t(ext->sky_width) * ext->sky_height * 3 * sizeof(float);
+        if (!ensure_buffer((void **)&c.sky, &c.cap_sky, bytes, error, error_len)) return false;
+        if (!check(cudaMemcpyAsync(c.sky, ext->sky_rgb, bytes, cudaMemcpyHostToDevice, c.stream), "sky upload", error, error_len))
+            return false;
+        S.sky_width = ext->sky_width;
+        S.sky_height = ext->sky_height;
+        S.sky_rgb = c.sky;
+    }
+    if (S.surrogate && ext) {
+        if (!surrogate_bind(ext->surrogate_model, S, error, error_len)) return false;
+    }
+    if (!ensure_buffer((void **)&c.scene, &c.cap_scene, sizeof(DeviceScene), error, error_len)) return false;
+    return check(cudaMemcpyAsync(c.scene, &S, sizeof(DeviceScene), cudaMemcpyHostToDevice, c.stream), "scene upload", error, error_len);
+}
+
+}  // namespace fpt
+
+using namespace fpt;
+
+namespace {
+
+// Render core shared by fpt_metal_render and fpt_cuda_render.
+int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const char *output_path, float *linear_output,
+                size_t linear_output_len, uint8_t *rgba_output, size_t rgba_output_len, double *elapsed_ms,
+                FptSdfProfileStats *profile_out, uint64_t *voxel_memory_bytes, uint32_t *voxel_active_bricks,
+                uint64_t *voxel_active_cells, double *build_ms, char *error, size_t error_len) {
+    if (elapsed_ms) *elapsed_ms = 0.0;
+    if (profile_out) std::memset(profile_out, 0, sizeof(*profile_out));
+    if (!config) { set_error(error, error_len, "missing render config"); return 1; }
+    if (config->width == 0 || config->height == 0) {
+        set_error(error, error_len, "invalid render size %ux%u", config->width, config->height);
+        return 1;
+    }
+    const size_t pixels = size_t(config->width) * config->height;
+    if (linear_output && linear_output_len < pixels * 4) {
+        set_error(error, error_len, "linear output buffer is too small (%zu < %zu)", linear_output_len, pixels * 4);
+        return 1;
+    }
+    if (rgba_output && rgba_output_len < pixels * 4) {
+        set_error(error, error_len, "rgba output buffer is too small (%zu < %zu)", rgba_output_len, pixels * 4);
+        return 1;
+    }
+    FptRenderConfig hydrated = *config;
+    if (!hydrate_hdri(hydrated, error, error_len)) return 1;
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    DeviceScene S;
+    if (!compile_scene(hydrated, ext, S, error, error_len)) return 1;
+    if (hydrated.renderer_backend == FPT_RENDERER_VOXEL) {
+        return voxel_render_core(hydrated, ext, S, output_path, linear_output, rgba_output, elapsed_ms, voxel_memory_bytes,
+                                 voxel_active_bricks, voxel_active_cells, build_ms, error, error_len);
+    }
+    if (hydrated.renderer_backend != FPT_RENDERER_SDF) {
+        set_error(error, error_len, "renderer backend %u is not supported by the CUDA path (research backends)",
+                  hydrated.renderer_backend);
+        return 1;
+    }
+    if (!upload_scene(S, ext, error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.accum, &c.cap_accum, pixels * sizeof(float4), error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.rgba, &c.cap_rgba, pixels * sizeof(uchar4), error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len)) return 1;
+    bool want_profile = profile_out != nullptr || hydrated.sdf_profile != 0u;
+    if (want_profile) {
+        if (!ensure_buffer((void **)&c.profile, &c.cap_profile, 8 * sizeof(unsigned long long), error, error_len)) return 1;
+        if (!check(cudaMemsetAsync(c.profile, 0, 8 * sizeof(unsigned long long), c.stream), "profile reset", error, error_len)) return 1;
+    }
+    cudaEventRecord(c.ev0, c.stream);
+    if (hydrated.focus_distance <= 0.0f) {
+        if (!check(launch_focus(S.kind, c.scene, c.stream), "focus-distance prepass", error, error_len)) return 1;
+    }
+    // Accumulation-mode policy (src/metal_bridge.mm:4531-4564).
+    const uint32_t spp = S.samples;
+    const bool auto_batch = spp <= 16u && hydrated.sdf_id != FPT_SDF_CAGE_FRACTAL;
+    const uint32_t mode = hydrated.sdf_accumulation_mode;
+    const bool batch = mode == FPT_SDF_ACCUMULATION_BATCH || (mode == FPT_SDF_ACCUMULATION_AUTO && auto_batch) || hydrated.preview;
+    const bool chunked = !batch && (mode == FPT_SDF_ACCUMULATION_CHUNKED || mode == FPT_SDF_ACCUMULATION_AUTO);
+    uint32_t step = batch ? spp : (chunked ? std::min(std::max(hydrated.sdf_chunk_samples, 1u), 64u) : 1u);
+    PathLaunch pl{};
+    pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height;
+    pl.accum = c.accum; pl.work_counter = c.counter; pl.grad_batch = c.grad_batch; pl.blocks = c.path_blocks;
+    pl.profile = want_profile ? c.profile : nullptr;
+    for (uint32_t start = 0; start < spp; start += step) {
+        pl.sample_begin = start;
+        pl.sample_end = std::min(spp, start + step);
+        if (!check(launch_pathtrace(pl, c.stream), "path-tracing launch", error, error_len)) return 1;
+    }
+    if (!check(launch_present(c.scene, S.width, S.height, c.accum, c.rgba, c.stream), "present launch", error, error_len)) return 1;
+    cudaEventRecord(c.ev1, c.stream);
+    if (!check(cudaStreamSynchronize(c.stream), "CUDA render", error, error_len)) return 1;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    if (elapsed_ms) *elapsed_ms = double(ms);
+    std::vector<uint8_t> host_rgba;
+    uint8_t *rgba = rgba_output;
+    if (!rgba) { host_rgba.resize(pixels * 4); rgba = host_rgba.data(); }
+    if (!check(cudaMemcpy(rgba, c.rgba, pixels * 4, cudaMemcpyDeviceToHost), "image readback", error, error_len)) return 1;
+    if (linear_output) {
+        if (!check(cudaMemcpy(linear_output, c.accum, pixels * sizeof(float4), cudaMemcpyDeviceToHost), "linear readback", error,
+                   error_len))
+            return 1;
+    }
+    if (want_profile && profile_out) {
+        unsigned long long v[8];
+        if (!check(cudaMemcpy(v, c.profile, sizeof(v), cudaMemcpyDeviceToHost), "profile readback", error, error_len)) return 1;
+        profile_out->primary_steps = v[0]; profile_out->secondary_steps = v[1]; profile_out->shadow_steps = v[2];
+        profile_out->normal_evals = v[3]; profile_out->bounces = v[4]; profile_out->pixels = v[5];
+        profile_out->distance_evals = v[6]; profile_out->material_evals = v[7];
+        profile_out->distance_evals_by_phase[0] = v[0];
+        profile_out->distance_evals_by_phase[1] = v[1];
+        profile_out->distance_evals_by_phase[2] = v[2];
+        profile_out->distance_evals_by_phase[3] = v[3];
+    }
+    if (output_path) {
+        if (unique_colour_sample(rgba, pixels) < 2) {
+            set_error(error, error_len, "render output is blank or single-colour");
+            return 1;
+        }
+        std::string err;
+        if (!write_png(output_path, config->width, config->height, rgba, err)) {
+            set_error(error, error_len, "%s", err.c_str());
+            return 1;
+        }
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fpt_metal_render(const char *metallib_path, const char *stitch_metallib_path, const char *stitch_archive_path,
+                     const char *output_path, const char *shader_source, size_t shader_source_len,
+                     const struct FptRenderConfig *config, double *build_ms, double *elapsed_ms, uint64_t *voxel_memory_bytes,
+                     uint32_t *voxel_active_bricks, uint64_t *voxel_active_cells, uint32_t *voxel_rejected_bricks,
+                     struct FptBoundGridStats *bound_grid_stats, uint32_t *stitch_cache_status,
+                     struct FptStitchValidationStats *stitch_validation_stats, struct FptStitchPipelineStats *stitch_pipeline_stats,
+                     struct FptSdfProfileStats *sdf_profile_stats, float *linear_output, size_t linear_output_len, char *error,
+                     size_t error_len) {
+    (void)metallib_path; (void)stitch_metallib_path; (void)stitch_archive_path; (void)shader_source; (void)shader_source_len;
+    if (build_ms) *build_ms = 0.0;
+    if (voxel_memory_bytes) *voxel_memory_bytes = 0;
+    if (voxel_active_bricks) *voxel_active_bricks = 0;
+    if (voxel_active_cells) *voxel_active_cells = 0;
+    if (voxel_rejected_bricks) *voxel_rejected_bricks = 0;
+    if (bound_grid_stats) std::memset(bound_grid_stats, 0, sizeof(*bound_grid_stats));
+    if (stitch_cache_status) *stitch_cache_status = 0;
+    if (stitch_validation_stats) std::memset(stitch_validation_stats, 0, sizeof(*stitch_validation_stats));
+    if (stitch_pipeline_stats) std::memset(stitch_pipeline_stats, 0, sizeof(*stitch_pipeline_stats));
+    if (!output_path) { set_error(error, error_len, "missing output path"); return 1; }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    return render_core(config, nullptr, output_path, linear_output, linear_output_len, nullptr, 0, elapsed_ms, sdf_profile_stats,
+                       voxel_memory_bytes, voxel_active_bricks, voxel_active_cells, build_ms, error, error_len);
+}
+
+int fpt_cuda_render(const struct FptRenderConfig *config, const struct FptCudaSceneExt *ext, const char *output_path,
+                    float *linear_output, size_t linear_output_len, uint8_t *rgba_output, size_t rgba_output_len,
+                    double *elapsed_ms, struct FptSdfProfileStats *profile, char *error, size_t error_len) {
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    return render_core(config, ext, output_path, linear_output, linear_output_len, rgba_output, rgba_output_len, elapsed_ms,
+                       profile, nullptr, nullptr, nullptr, nullptr, error, error_len);
+}
+
+int fpt_cuda_trace_primary(const struct FptRenderConfig *config, const struct FptCudaSceneExt *ext, struct FptCudaPrimaryHit *hits,
+                           size_t hit_count, double *elapsed_ms, char *error, size_t error_len) {
+    if (elapsed_ms) *elapsed_ms = 0.0;
+    if (!config || !hits) { set_error(error, error_len, "missing primary-ray input"); return 1; }
+    if (config->width == 0 || config->height == 0) {
+        set_error(error, error_len, "invalid render size %ux%u", config->width, config->height);
+        return 1;
+    }
+    size_t pixels = size_t(config->width) * config->height;
+    if (hit_count < pixels) { set_error(error, error_len, "hit buffer is too small (%zu < %zu)", hit_count, pixels); return 1; }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    FptRenderConfig hydrated = *config;
+    if (!hydrate_hdri(hydrated, error, error_len)) return 1;
+    DeviceScene S;
+    if (!compile_scene(hydrated, ext, S, error, error_len)) return 1;
+    if (!upload_scene(S, ext, error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.hits, &c.cap_hits, pixels * sizeof(FptCudaPrimaryHit), error, error_len)) return 1;
+    cudaEventRecord(c.ev0, c.stream);
+    if (!check(launch_trace_primary(S.kind, c.scene, S.width, S.height, c.hits, c.stream), "primary-ray launch", error, error_len))
+        return 1;
+    cudaEventRecord(c.ev1, c.stream);
+    if (!check(cudaStreamSynchronize(c.stream), "primary-ray trace", error, error_len)) return 1;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    if (elapsed_ms) *elapsed_ms = ms;
+    return check(cudaMemcpy(hits, c.hits, pixels * sizeof(FptCudaPrimaryHit), cudaMemcpyDeviceToHost), "hit readback", error,
+                 error_len) ? 0 : 1;
+}
+
+int fpt_mandelbulber_sample_field(const char *metallib_path, const char *shader_source, size_t shader_source_len,
+                                  const struct FptRenderConfig *config, const float *points_xyzw, size_t point_count,
+                                  struct FptMandelbulberFieldSample *samples, char *error, size_t error_len) {
+    (void)metallib_path; (void)shader_source; (void)shader_source_len;
+    if (!config || !points_xyzw || !samples || point_count == 0u) {
+        set_error(error, error_len, "missing Mandelbulber field-sampling input");
+        return 1;
+    }
+    if (config->sdf_id != FPT_SDF_MANDELBULBER) {
+        set_error(error, error_len, "field sampling requires a Mandelbulber scene");
+        return 1;
+    }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    DeviceScene S;
+    if (!compile_scene(*config, nullptr, S, error, error_len)) return 1;
+    if (!upload_scene(S, nullptr, error, error_len)) return 1;
+    size_t bytes = point_count * sizeof(float4);
+    if (!ensure_buffer((void **)&c.points, &c.cap_points, bytes, error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.samples, &c.cap_samples, bytes, error, error_len)) return 1;
+    if (!check(cudaMemcpyAsync(c.points, points_xyzw, bytes, cudaMemcpyHostToDevice, c.stream), "point upload", error, error_len))
+        return 1;
+    if (!check(launch_field_sample(c.scene, c.points, c.samples, point_count, c.stream), "field-sampling launch", error, error_len))
+        return 1;
+    if (!check(cudaStreamSynchronize(c.stream), "Mandelbulber field-sampling dispatch", error, error_len)) return 1;
+    return check(cudaMemcpy(samples, c.samples, bytes, cudaMemcpyDeviceToHost), "sample readback", error, error_len) ? 0 : 1;
+}
+
+int fpt_cuda_sample_distance(const struct FptRenderConfig *config, const struct FptCudaSceneExt *ext, const float *points_xyzw,
+                             size_t point_count, float *samples, float *gradients, char *error, size_t error_len) {
+    if (!config || !points_xyzw || !samples || point_count == 0u) {
+        set_error(error, error_len, "missing distance-sampling input");
+        return 1;
+    }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    DeviceScene S;
+    if (!compile_scene(*config, ext, S, error, error_len)) return 1;
+    if (!upload_scene(S, ext, error, error_len)) return 1;
+    size_t bytes = point_count * sizeof(float4);
+    if (!ensure_buffer((void **)&c.points, &c.cap_points, bytes, error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.samples, &c.cap_samples, bytes, error, error_len)) return 1;
+    if (gradients && !ensure_buffer((void **)&c.grads, &c.cap_grads, point_count * 3 * sizeof(float), error, error_len)) return 1;
+    if (!check(cudaMemcpyAsync(c.points, points_xyzw, bytes, cudaMemcpyHostToDevice, c.stream), "point upload", error, error_len))
+        return 1;
+    if (!check(launch_sample_distance(S.kind, c.scene, c.points, c.samples, gradients ? c.grads : nullptr, point_count, c.stream),
+               "distance-sampling launch", error, error_len))
+        return 1;
+    if (!check(cudaStreamSynchronize(c.stream), "distance sampling", error, error_len)) return 1;
+    if (!check(cudaMemcpy(samples, c.samples, bytes, cudaMemcpyDeviceToHost), "sample readback", error, error_len)) return 1;
+    if (gradients &&
+        !check(cudaMemcpy(gradients, c.grads, point_count * 3 * sizeof(float), cudaMemcpyDeviceToHost), "gradient readback", error,
+               error_len))
+        return 1;
+    return 0;
+}
+
+int fpt_compare_images(const char *baseline_path, const char *candidate_path, const char *report_path, char *error,
+                       size_t error_len) {
+    if (!baseline_path || !candidate_path || !report_path) { set_error(error, error_len, "missing comparison path"); return 1; }
+    Image a, b;
+    std::string err;
+    if (!read_png(baseline_path, a, err) || !read_png(candidate_path, b, err)) { set_error(error, error_len, "%s", err.c_str()); return 1; }
+    if (a.width != b.width || a.height != b.height) {
+        set_error(error, error_len, "dimension mismatch: baseline %ux%u candidate %ux%u", a.width, a.height, b.width, b.height);
+        return 1;
+    }
+    ImageMetrics m = compare_rgba(a.rgba.data(), b.rgba.data(), a.width, a.height);
+    FILE *f = std::fopen(report_path, "w");
+    if (!f) { set_error(error, error_len, "failed to open report %s", report_path); return 1; }
+    std::fprintf(f,
+                 "{\n  \"baseline\": \"%s\",\n  \"candidate\": \"%s\",\n  \"width\": %u,\n  \"height\": %u,\n"
+                 "  \"mean_absolute_error\": %.17g,\n  \"root_mean_square_error\": %.17g,\n  \"luminance_ssim\": %.17g,\n"
+                 "  \"low_frequency_luminance_ssim\": %.17g,\n  \"max_absolute_error\": %.0f,\n  \"changed_pixel_percent\": %.17g,\n"
+                 "  \"unique_colours\": {\n    \"baseline\": %zu,\n    \"candidate\": %zu\n  }\n}\n",
+                 baseline_path, candidate_path, a.width, a.height, m.mae, m.rmse, m.ssim, m.lf_ssim, m.max_abs, m.changed_pct,
+                 m.unique_baseline, m.unique_candidate);
+    std::fclose(f);
+    return 0;
+}
+
+int fpt_metal_device_name(char *name, size_t name_len) {
+    if (!name || name_len == 0) return 1;
+    int dev = 0, count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) { name[0] = 0; return 1; }
+    cudaGetDevice(&dev);
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) { name[0] = 0; return 1; }
+    std::snprintf(name, name_len, "%s", p.name);
+    return 0;
+}
+
+int fpt_test_async_stitch_context(const char *metallib_path, const char *stitch_metallib_path, const char *stitch_archive_path,
+                                  const struct FptRenderConfig *config, struct FptAsyncJitStats *stats, char *error,
+                                  size_t error_len) {
+    (void)metallib_path; (void)stitch_metallib_path; (void)stitch_archive_path; (void)config;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    set_error(error, error_len, "unsupported: the CUDA path has no runtime shader-stitching JIT");
+    return 1;
+}
+
+int fpt_metal_preview(const char *metallib_path, const char *stitch_metallib_path, const char *const *stitch_archive_paths,
+                      const char *shader_source, size_t shader_source_len, const struct FptRenderConfig *config,
+                      const struct FptRenderConfig *scene_configs, uint32_t scene_config_count, uint32_t scene_config_index,
+                      char *error, size_t error_len) {
+    (void)metallib_path; (void)stitch_metallib_path; (void)stitch_archive_paths; (void)shader_source; (void)shader_source_len;
+    (void)config; (void)scene_configs; (void)scene_config_count; (void)scene_config_index;
+    set_error(error, error_len, "unsupported: interactive preview needs a window system, which a headless CUDA node lacks");
+    return 1;
+}
+
+}  // extern "C"

@@ -1,0 +1,52 @@
+// bridge_internal.h -- state and helpers shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <mutex>
+
+#include "fpt_scene.h"
+
+namespace fpt {
+
+// Process-wide CUDA state.  Device buffers are grown on demand and reused
+// across calls; calls are serialised by `mutex`.
+struct Context {
+    std::mutex mutex;
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    DeviceScene *scene = nullptr; size_t cap_scene = 0;
+    float4 *accum = nullptr; size_t cap_accum = 0;
+    uchar4 *rgba = nullptr; size_t cap_rgba = 0;
+    unsigned int *counter = nullptr; size_t cap_counter = 0;
+    unsigned long long *profile = nullptr; size_t cap_profile = 0;
+    float *sky = nullptr; size_t cap_sky = 0;
+    FptCudaPrimaryHit *hits = nullptr; size_t cap_hits = 0;
+    float4 *points = nullptr; size_t cap_points = 0;
+    float4 *samples = nullptr; size_t cap_samples = 0;
+    float *grads = nullptr; size_t cap_grads = 0;
+    // launch tuning (set by the autotuner entry point; 0 = defaults)
+    uint32_t grad_batch = 0;
+    int path_blocks = 0;
+};
+
+Context &ctx();
+void set_error(char *error, size_t error_len, const char *fmt, ...);
+bool ensure_device(char *error, size_t error_len);
+bool ensure_buffer(void **ptr, size_t *cap, size_t need, char *error, size_t error_len);
+bool check(cudaError_t e, const char *what, char *error, size_t error_len);
+bool compile_scene(const FptRenderConfig &c, const FptCudaSceneExt *ext, DeviceScene &S, char *error, size_t error_len);
+bool hydrate_hdri(FptRenderConfig &config, char *error, size_t error_len);
+bool upload_scene(DeviceScene &S, const FptCudaSceneExt *ext, char *error, size_t error_len);
+uint32_t scene_kind(const FptCudaSceneExt &e);
+
+// voxel.cu
+int voxel_render_core(const FptRenderConfig &config, const FptCudaSceneExt *ext, DeviceScene &S, const char *output_path,
+                      float *linear_output, uint8_t *rgba_output, double *elapsed_ms, uint64_t *voxel_memory_bytes,
+                      uint32_t *voxel_active_bricks, uint64_t *voxel_active_cells, double *build_ms, char *error,
+                      size_t error_len);
+// mlp.cu
+bool surrogate_bind(uint64_t model, DeviceScene &S, char *error, size_t error_len);
+
+}  // namespace fpt

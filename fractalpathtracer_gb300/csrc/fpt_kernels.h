@@ -1,0 +1,32 @@
+// fpt_kernels.h -- host-side launchers of the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "fpt_scene.h"
+
+namespace fpt {
+
+struct PathLaunch {
+    const DeviceScene *scene;   // device pointer
+    uint32_t kind;              // SceneKind
+    uint32_t width, height;
+    float4 *accum;              // width*height, running mean
+    unsigned int *work_counter; // device scratch word
+    uint32_t sample_begin, sample_end;
+    uint32_t grad_batch;        // 0 = default
+    int blocks;                 // persistent grid size, <= 0 = one wave of resident blocks
+    unsigned long long *profile;  // 8 device counters or null
+};
+
+cudaError_t launch_pathtrace(const PathLaunch &pl, cudaStream_t stream);
+cudaError_t launch_trace_primary(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, FptCudaPrimaryHit *hits,
+                                 cudaStream_t stream);
+cudaError_t launch_focus(uint32_t kind, DeviceScene *scene, cudaStream_t stream);
+cudaError_t launch_field_sample(const DeviceScene *scene, const float4 *pts, float4 *out, size_t n, cudaStream_t stream);
+cudaError_t launch_sample_distance(uint32_t kind, const DeviceScene *scene, const float4 *pts, float4 *out, float *grads, size_t n,
+                                   cudaStream_t stream);
+cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out,
+                           cudaStream_t stream);
+
+}  // namespace fpt

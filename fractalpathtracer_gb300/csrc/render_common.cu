@@ -1,0 +1,119 @@
+// render_common.cu -- present kernel and the per-kind dispatch of the launchers.
+#include "render_impl.cuh"
+
+namespace fpt {
+
+// ---------------------------------------------------------------- present
+// present_kernel (shaders/Shaders.metal:8012-8025) with highlightAt
+// (7466-7481), sampleAccumBilinear (7483-7496), chromaticAt (7498-7507),
+// postProcess/toneMap (6778-6825) and the vertical flip of outputIndex.
+__device__ __forceinline__ float3 gamma_srgb(float3 l) {
+    float3 o;
+    o.x = l.x <= 0.0031308f ? l.x * 12.92f : 1.055f * powf(fmaxf(l.x, 0.0f), 1.0f / 2.4f) - 0.055f;
+    o.y = l.y <= 0.0031308f ? l.y * 12.92f : 1.055f * powf(fmaxf(l.y, 0.0f), 1.0f / 2.4f) - 0.055f;
+    o.z = l.z <= 0.0031308f ? l.z * 12.92f : 1.055f * powf(fmaxf(l.z, 0.0f), 1.0f / 2.4f) - 0.055f;
+    return o;
+}
+__device__ __forceinline__ float aces1(float x) { return clampf((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f, 1.0f); }
+__device__ float3 pbr_neutral(float3 c) {
+    float x = fminf(c.x, fminf(c.y, c.z));
+    float off = x < 0.08f ? x - 6.25f * x * x : 0.04f;
+    c = c - off;
+    float peak = maxc3(c);
+    if (peak < 0.76f) return c;
+    float d = 1.0f - 0.76f;
+    float np = 1.0f - d * d / (peak + d - 0.76f);
+    c = c * (np / peak);
+    float g = 1.0f - 1.0f / (0.15f * (peak - np) + 1.0f);
+    return mix3(c, mk3(np), g);
+}
+__device__ float3 post_process(float3 c, const DeviceScene &S) {
+    float n = S.post[0];
+    if (n == 0.0f) c = gamma_srgb(c);
+    else if (n == 1.0f) c = mk3(powf(c.x, 1.0f / 2.4f), powf(c.y, 1.0f / 2.4f), powf(c.z, 1.0f / 2.4f));
+    else if (n == 2.0f) c = mk3(powf(c.x, 1.0f / 2.6f), powf(c.y, 1.0f / 2.6f), powf(c.z, 1.0f / 2.6f));
+    else if (n == 3.0f) c = mk3(aces1(c.x), aces1(c.y), aces1(c.z));
+    else if (n == 4.0f) c = pbr_neutral(c);
+    c = c * S.post[1] + S.post[2];
+    c = (c - mk3(0.5f)) * S.post[4] + mk3(0.5f);
+    float l = dot(c, mk3(0.2126f, 0.7152f, 0.0722f));
+    c = mix3(mk3(l), c, S.post[3]);
+    return clamp3(c, 0.0f, 1.0f);
+}
+__global__ void __launch_bounds__(256) present_kernel(const DeviceScene *scene, const float4 *accum, uchar4 *out) {
+    const DeviceScene &S = *scene;
+    uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u), y = blockIdx.y * 8u + (threadIdx.x >> 5);
+    const uint32_t W = S.width, H = S.height;
+    if (x >= W || y >= H) return;
+    auto A = [&](uint32_t X, uint32_t Y) { float4 a = accum[size_t(Y) * W + X]; return mk3(a.x, a.y, a.z); };
+    auto bil = [&](float u, float v) {
+        float px = clampf(u, 0.0f, 1.0f) * float(W) - 0.5f, py = clampf(v, 0.0f, 1.0f) * float(H) - 0.5f;
+        int bx = int(floorf(px)), by = int(floorf(py));
+        float fx = fractf(px), fy = fractf(py);
+        uint32_t x0 = uint32_t(min(max(bx, 0), int(W - 1))), y0 = uint32_t(min(max(by, 0), int(H - 1)));
+        uint32_t x1 = min(x0 + 1u, W - 1u), y1 = min(y0 + 1u, H - 1u);
+        return mix3(mix3(A(x0, y0), A(x1, y0), fx), mix3(A(x0, y1), A(x1, y1), fx), fy);
+    };
+    float u = (float(x) + 0.5f) / float(W), v = (float(y) + 0.5f) / float(H);
+    float dx = u - 0.5f, dy = v - 0.5f;
+    float len = sqrtf(dx * dx + dy * dy);
+    float ox = dx * S.post[5] * len / 8.0f, oy = dy * S.post[5] * len / 8.0f;
+    float3 center = bil(u, v), col = center;
+    if (fabsf(S.post[5]) > 0.00001f) {
+        float3 g = bil(u - ox, v - oy), b = bil(u - 2.0f * ox, v - 2.0f * oy);
+        col = mk3(center.x, g.y, b.z);
+    }
+    float3 hl = mk3(0.0f);
+    if (S.post[6] > 0.00001f) {
+        uint32_t x0 = x > 0 ? x - 1 : x, x1 = min(x + 1, W - 1), y0 = y > 0 ? y - 1 : y, y1 = min(y + 1, H - 1);
+        float3 br = max3(A(x, y) - mk3(0.5f), mk3(0.0f));
+        br = br + A(x1, y) * 0.25f + A(x0, y) * 0.25f + A(x, y1) * 0.25f + A(x, y0) * 0.25f;
+        hl = br * S.post[6];
+    }
+    float3 o = post_process(col + hl, S);
+    out[size_t(H - 1 - y) * W + x] = make_uchar4((unsigned char)(clampf(o.x, 0.f, 1.f) * 255.0f),
+                                                 (unsigned char)(clampf(o.y, 0.f, 1.f) * 255.0f),
+                                                 (unsigned char)(clampf(o.z, 0.f, 1.f) * 255.0f), 255);
+}
+
+
+cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out, cudaStream_t st) {
+    dim3 grid((W + 31u) / 32u, (H + 7u) / 8u);
+    present_kernel<<<grid, 256, 0, st>>>(scene, accum, out);
+    return cudaGetLastError();
+}
+
+#define FPT_DECLARE_KIND(n)                                                                                                 \
+    cudaError_t launch_pathtrace_k##n(const PathLaunch &, cudaStream_t);                                                    \
+    cudaError_t launch_trace_primary_k##n(const DeviceScene *, uint32_t, uint32_t, FptCudaPrimaryHit *, cudaStream_t);        \
+    cudaError_t launch_focus_k##n(DeviceScene *, cudaStream_t);                                                              \
+    cudaError_t launch_sample_distance_k##n(const DeviceScene *, const float4 *, float4 *, float *, size_t, cudaStream_t);
+FPT_DECLARE_KIND(0)
+FPT_DECLARE_KIND(1)
+FPT_DECLARE_KIND(2)
+FPT_DECLARE_KIND(3)
+FPT_DECLARE_KIND(4)
+FPT_DECLARE_KIND(5)
+
+#define FPT_DISPATCH(kind, fn, ...)                            \
+    switch (kind) {                                            \
+        case KIND_BULB8: return fn##1(__VA_ARGS__);            \
+        case KIND_BULB: return fn##2(__VA_ARGS__);             \
+        case KIND_BOX: return fn##3(__VA_ARGS__);              \
+        case KIND_MENGER: return fn##4(__VA_ARGS__);           \
+        case KIND_HYBRID: return fn##5(__VA_ARGS__);           \
+        default: return fn##0(__VA_ARGS__);                    \
+    }
+
+cudaError_t launch_pathtrace(const PathLaunch &pl, cudaStream_t stream) { FPT_DISPATCH(pl.kind, launch_pathtrace_k, pl, stream) }
+cudaError_t launch_trace_primary(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, FptCudaPrimaryHit *hits,
+                                 cudaStream_t st) {
+    FPT_DISPATCH(kind, launch_trace_primary_k, scene, W, H, hits, st)
+}
+cudaError_t launch_focus(uint32_t kind, DeviceScene *scene, cudaStream_t st) { FPT_DISPATCH(kind, launch_focus_k, scene, st) }
+cudaError_t launch_sample_distance(uint32_t kind, const DeviceScene *scene, const float4 *pts, float4 *out, float *grads, size_t n,
+                                   cudaStream_t st) {
+    FPT_DISPATCH(kind, launch_sample_distance_k, scene, pts, out, grads, n, st)
+}
+
+}  // namespace fpt

@@ -1,0 +1,655 @@
+/*
+ * fpt_cuda.h -- C ABI of the GB300 (sm_103a) sphere-tracing path.
+ *
+ * This header is the drop-in seam for FPT Metal's bridge.  The first block
+ * declares the structs and entry points of the reference interface with the
+ * same names, member order and sizes (reference: src/metal_bridge.h:1-490,
+ * mirrored in Rust by src/ffi.rs:89-488, sizes pinned by src/ffi.rs:494-507),
+ * so a Rust build that links libfpt_cuda.so instead of fpt_metal_bridge keeps
+ * its `extern "C"` declarations unchanged.  The second block declares the
+ * side entry points this library adds for per-ray output, voxel bricks, DDA
+ * cell sequences, batched scenes and the learned distance surrogate.
+ *
+ * Conventions shared by every entry point (reference: src/metal_bridge.mm:41-47,
+ * 4322-4361):
+ *   - return 0 on success, 1 on failure;
+ *   - on failure a NUL-terminated message is written into error[0..error_len);
+ *   - out-parameters are zeroed on entry;
+ *   - every pointer is owned by the caller and is not retained after return;
+ *   - calls are synchronous and must be serialised by the caller (one call in
+ *     flight per process), as the reference's Rust side does with a mutex.
+ */
+#ifndef FPT_CUDA_H
+#define FPT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------- */
+/* Reference interface (src/metal_bridge.h)                                  */
+/* ------------------------------------------------------------------------- */
+
+/* Scene selector values of FptRenderConfig.sdf_id (src/metal_bridge.h:10-24). */
+typedef enum FptSdfId {
+    FPT_SDF_CORNELL_BOX = 0,
+    FPT_SDF_GLASS_BALL = 1,
+    FPT_SDF_BALL_FRACTAL = 2,
+    FPT_SDF_CAGE_FRACTAL = 3,
+    FPT_SDF_IFS_FRACTAL = 4,
+    FPT_SDF_MANDELBOX_FRACTAL = 5,
+    FPT_SDF_MENGER_SPONGE = 6,
+    FPT_SDF_TOWER_FRACTAL = 7,
+    FPT_SDF_TREE_FRACTAL = 8,
+    FPT_SDF_PROGRAM = 9,
+    FPT_SDF_README_CORNELL = 10,
+    FPT_SDF_README_GLASS = 11,
+    FPT_SDF_MANDELBULBER = 12,
+} FptSdfId;
+
+enum {
+    FPT_SDF_PROGRAM_MAX_OPS = 64,
+    FPT_SDF_FLAT_UNION_MAX_PRIMITIVES = 64,
+    FPT_SDF_GRADIENT_MAX_STOPS = 16,
+    FPT_HDRI_PATH_CAPACITY = 256,
+    FPT_HDRI_LUT_WIDTH = 32,
+    FPT_HDRI_LUT_HEIGHT = 16,
+};
+
+enum {
+    FPT_SDF_STITCH_STATE_FULL = 0,
+    FPT_SDF_STITCH_STATE_LEAN = 1,
+};
+
+/* Typed SDF program opcodes (src/metal_bridge.h:40-56). */
+typedef enum FptSdfOpcode {
+    FPT_SDF_OP_ABS = 1,
+    FPT_SDF_OP_TRANSLATE = 2,
+    FPT_SDF_OP_SCALE = 3,
+    FPT_SDF_OP_ROTATE_X = 4,
+    FPT_SDF_OP_ROTATE_Y = 5,
+    FPT_SDF_OP_ROTATE_Z = 6,
+    FPT_SDF_OP_REPEAT = 7,
+    FPT_SDF_OP_SORT_DESC = 8,
+    FPT_SDF_OP_SPHERE = 16,
+    FPT_SDF_OP_BOX = 17,
+    FPT_SDF_OP_PLANE = 18,
+    FPT_SDF_OP_UNION = 24,
+    FPT_SDF_OP_INTERSECTION = 25,
+    FPT_SDF_OP_SUBTRACT = 26,
+    FPT_SDF_OP_ORBIT_ADD = 32,
+} FptSdfOpcode;
+
+/* One typed-program instruction, 32 bytes (src/metal_bridge.h:58-64). */
+struct FptSdfInstruction {
+    uint32_t opcode;
+    uint32_t flags;          /* combine mode: 0 union, 1 intersection, 2 subtract */
+    uint32_t material_index;
+    uint32_t _pad0;
+    float data[4];
+};
+
+struct FptPrimitiveInstance {
+    float transform[12];
+    float data[4];
+    uint32_t opcode;
+    float distance_scale;
+    uint32_t source_instruction;
+    uint32_t _pad0;
+};
+
+struct FptAffineTransform {
+    float transform[12];
+    float distance_scale;
+    uint32_t _pad0[3];
+};
+
+struct FptIndexedPrimitive {
+    float data[4];
+    uint32_t opcode;
+    uint32_t transform_index;
+    uint32_t source_instruction;
+    uint32_t combine_mode;
+};
+
+struct FptTypedSoAProgram {
+    uint32_t sphere_count;
+    uint32_t box_count;
+    uint32_t plane_count;
+    uint32_t _pad0;
+    float sphere_x[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float sphere_y[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float sphere_z[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float sphere_radius[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    uint32_t sphere_source[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float box_x[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float box_y[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float box_z[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float box_half_x[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float box_half_y[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float box_half_z[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    uint32_t box_source[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float plane_x[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float plane_y[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float plane_z[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float plane_center_x[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float plane_center_y[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float plane_center_z[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    float plane_offset[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    uint32_t plane_source[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+};
+
+typedef enum FptSdfAccumulationMode {
+    FPT_SDF_ACCUMULATION_AUTO = 0,
+    FPT_SDF_ACCUMULATION_PER_SAMPLE = 1,
+    FPT_SDF_ACCUMULATION_BATCH = 2,
+    FPT_SDF_ACCUMULATION_CHUNKED = 3,
+} FptSdfAccumulationMode;
+
+typedef enum FptRendererBackend {
+    FPT_RENDERER_SDF = 0,
+    FPT_RENDERER_VOXEL = 1,
+    FPT_RENDERER_BOUND_GRID = 2,
+    FPT_RENDERER_REGIONAL = 3,
+} FptRendererBackend;
+
+typedef enum FptVoxelNormalMode {
+    FPT_VOXEL_NORMAL_FACE = 0,
+    FPT_VOXEL_NORMAL_SMOOTH = 1,
+    FPT_VOXEL_NORMAL_EXACT = 2,
+} FptVoxelNormalMode;
+
+typedef enum FptVoxelMaterialMode {
+    FPT_VOXEL_MATERIAL_STORED = 0,
+    FPT_VOXEL_MATERIAL_EXACT = 1,
+} FptVoxelMaterialMode;
+
+typedef enum FptVoxelOffsetMode {
+    FPT_VOXEL_OFFSET_LEGACY = 0,
+    FPT_VOXEL_OFFSET_PRECISION = 1,
+} FptVoxelOffsetMode;
+
+typedef enum FptVoxelStorage {
+    FPT_VOXEL_STORAGE_DENSE = 0,
+    FPT_VOXEL_STORAGE_SPARSE_BRICKS = 1,
+    FPT_VOXEL_STORAGE_TEMPLATE_BRICKS = 3,
+} FptVoxelStorage;
+
+typedef enum FptVoxelCoverageMode {
+    FPT_VOXEL_COVERAGE_LEGACY = 0,
+    FPT_VOXEL_COVERAGE_LIPSCHITZ = 1,
+    FPT_VOXEL_COVERAGE_INTERVAL = 2,
+} FptVoxelCoverageMode;
+
+typedef enum FptVoxelBuildMode {
+    FPT_VOXEL_BUILD_STAGING = 0,
+    FPT_VOXEL_BUILD_DIRECT = 1,
+} FptVoxelBuildMode;
+
+typedef enum FptVoxelLeafRefinement {
+    FPT_VOXEL_LEAF_REFINEMENT_NONE = 0,
+    FPT_VOXEL_LEAF_REFINEMENT_SECANT_BISECTION = 1,
+    FPT_VOXEL_LEAF_REFINEMENT_RESTRICTED_TRACE = 2,
+    FPT_VOXEL_LEAF_REFINEMENT_FIXED_DE = 3,
+} FptVoxelLeafRefinement;
+
+/* Whole-render parameter block, 30448 bytes (src/metal_bridge.h:170-267;
+ * size asserted at src/metal_bridge.mm:36).  Member meaning follows the
+ * reference: render[0] bounces, render[1] march steps, render[2] normal
+ * epsilon, render[3] minimum distance, render[4] maximum distance,
+ * render[5] fog-LOD mix, render[6] distance halving, render[7] slow-shading
+ * stencil; world/sun/post as in src/scene.rs:743-778. */
+struct FptRenderConfig {
+    uint32_t width;
+    uint32_t height;
+    uint32_t samples;
+    uint32_t preview;
+    uint32_t sdf_id;
+    uint32_t glass_mode;
+    uint32_t sdf_accumulation_mode;
+    uint32_t sdf_profile;
+    uint32_t sdf_bounce_cap;
+    uint32_t sdf_russian_roulette;
+    uint32_t sdf_normal_mode;
+    uint32_t sdf_chunk_samples;
+    float sdf_rr_start;
+    float sdf_rr_min_prob;
+    float mandel_iteration_scale;
+
+    float camera_position[3];
+    float camera_yaw_pitch[2];
+    float camera_roll;
+    float camera_fov;
+    float camera_dof;
+    float focus_distance;
+
+    float render[8];
+    float world[7];
+    float world_one_color[3];
+    float sun[5];
+    float sun_color[3];
+    float background_gradient[6];
+    float post[7];
+    float set_values[40];
+    float vset_values[133];
+
+    uint32_t sdf_program_count;
+    uint32_t gradient_count;
+    uint32_t material_mode;
+    uint32_t hdri_enabled;
+    uint32_t hdri_width;
+    uint32_t hdri_height;
+    uint32_t _pad_hdri[2];
+    uint32_t fractal_style_mode;
+    uint32_t _pad_style[3];
+    float fractal_style[12];
+    float program_material[8];
+    struct FptSdfInstruction sdf_program[FPT_SDF_PROGRAM_MAX_OPS];
+    float gradient_stops[FPT_SDF_GRADIENT_MAX_STOPS][4];
+    uint8_t hdri_path[FPT_HDRI_PATH_CAPACITY];
+    uint16_t hdri_lut[FPT_HDRI_LUT_WIDTH * FPT_HDRI_LUT_HEIGHT * 3];
+    uint32_t renderer_backend;
+    uint32_t voxel_resolution;
+    uint32_t voxel_normal_mode;
+    uint32_t voxel_storage;
+    float voxel_bounds_min[3];
+    float voxel_surface_band;
+    float voxel_bounds_max[3];
+    uint32_t voxel_fill_interior;
+    uint32_t voxel_coverage_mode;
+    uint32_t voxel_build_mode;
+    uint32_t voxel_brick_rejection;
+    uint32_t voxel_leaf_refinement;
+    uint32_t voxel_material_mode;
+    uint32_t voxel_offset_mode;
+    uint32_t bound_grid_resolution;
+    uint32_t bound_grid_profile;
+    uint32_t bound_grid_profile_stride;
+    uint32_t bound_grid_cage_bounds;
+    uint32_t bound_grid_directional;
+    uint32_t sdf_program_source_count;
+    uint32_t sdf_program_optimization;
+    uint32_t regional_program_resolution;
+    uint32_t bound_grid_fp16;
+    uint32_t sdf_flat_union_count;
+    struct FptPrimitiveInstance sdf_flat_union_instances[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    uint32_t sdf_shading_program_count;
+    uint32_t sdf_geometry_split;
+    struct FptSdfInstruction sdf_shading_program[FPT_SDF_PROGRAM_MAX_OPS];
+    uint32_t sdf_topology_specialization;
+    uint32_t sdf_runtime_source_bytecode;
+    uint32_t sdf_function_stitching;
+    uint32_t sdf_stitched_surface;
+    uint32_t sdf_stitch_validation;
+    uint32_t sdf_stitch_distance_only;
+    uint32_t sdf_stitch_split_graph;
+    uint32_t sdf_stitch_fusion;
+    uint32_t sdf_canonical_count;
+    uint32_t sdf_canonical_source_count;
+    struct FptPrimitiveInstance sdf_canonical_primitives[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    uint32_t sdf_canonical_transform_count;
+    uint32_t _pad_canonical_indexed[3];
+    struct FptAffineTransform sdf_canonical_transforms[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    struct FptIndexedPrimitive sdf_indexed_primitives[FPT_SDF_FLAT_UNION_MAX_PRIMITIVES];
+    struct FptTypedSoAProgram sdf_typed_soa;
+};
+
+struct FptBoundGridStats {
+    uint64_t macro_cells[3];
+    uint64_t certified_skips[3];
+    uint64_t candidate_intervals[3];
+    uint64_t candidate_misses[3];
+    uint64_t candidate_hits[3];
+    uint64_t unknown_intervals[3];
+    uint64_t field_evaluations[3];
+    uint64_t directional_steps[3];
+    uint64_t cell_exit_clamps[3];
+    uint64_t unknown_derivative_intervals[3];
+    uint64_t profiled_paths;
+    uint64_t certified_cells;
+    uint64_t unknown_cells;
+    uint64_t sampled_bound_failures;
+    uint64_t sampled_false_skips;
+    uint64_t certified_derivative_cells;
+    uint64_t unknown_derivative_cells;
+    uint64_t sampled_derivative_failures;
+    uint64_t regional_cells;
+    uint64_t regional_fallback_cells;
+    uint64_t regional_unique_programs;
+    uint64_t regional_retained_instructions;
+    uint64_t regional_sampled_distance_failures;
+    uint64_t regional_profiled_paths;
+    uint64_t regional_distance_evaluations[3];
+    uint64_t regional_atlas_evaluations[3];
+    uint64_t regional_full_program_evaluations[3];
+    uint64_t regional_cell_entries[3];
+    uint64_t regional_same_cell_reuses[3];
+    uint64_t regional_same_program_reuses[3];
+    uint64_t regional_program_id_loads[3];
+    uint64_t regional_header_loads[3];
+    uint64_t regional_dynamic_instructions[3];
+    uint64_t regional_pruned_cells;
+    uint64_t regional_pruned_primitives;
+    uint64_t regional_repeat_seam_fallback_cells;
+    uint64_t regional_unsupported_fallback_cells;
+    uint64_t regional_no_dominance_cells;
+};
+
+struct FptStitchValidationStats {
+    uint64_t sample_count;
+    uint64_t distance_failures;
+    uint64_t gradient_failures;
+    float max_distance_error;
+    float max_gradient_error;
+};
+
+struct FptStitchPipelineStats {
+    uint32_t instruction_count;
+    uint32_t transform_instruction_count;
+    uint32_t primitive_instruction_count;
+    uint32_t primitive_type_runs;
+    uint32_t union_count;
+    uint32_t intersection_count;
+    uint32_t subtraction_count;
+    uint32_t thread_execution_width;
+    uint32_t max_total_threads_per_threadgroup;
+    uint32_t graph_node_count;
+    uint64_t static_threadgroup_memory_bytes;
+    uint64_t runtime_source_bytes;
+    double runtime_library_compile_ms;
+    double runtime_pipeline_link_ms;
+};
+
+struct FptSdfProfileStats {
+    uint64_t primary_steps;
+    uint64_t secondary_steps;
+    uint64_t shadow_steps;
+    uint64_t normal_evals;
+    uint64_t bounces;
+    uint64_t pixels;
+    uint64_t distance_evals;
+    uint64_t march_orbit_iterations;
+    uint64_t refinement_steps;
+    uint64_t normal_field_evals;
+    uint64_t material_evals;
+    uint64_t max_ray_steps;
+    uint64_t max_pixel_steps;
+    uint64_t distance_evals_by_phase[4];
+    uint64_t orbit_iterations_by_phase[4];
+    uint64_t formula_slot_iterations[9];
+    uint64_t refinement_distance_evals;
+    double primary_ms_estimate;
+    double secondary_ms_estimate;
+    double shadow_ms_estimate;
+    double normal_ms_estimate;
+    double bounce_ms_estimate;
+};
+
+struct FptAsyncJitStats {
+    double fallback_render_ms;
+    double jit_build_ms;
+    double stitched_render_ms;
+    uint32_t cache_status;
+    uint32_t fallback_completed_before_jit;
+    float max_absolute_error;
+    uint32_t _pad0;
+};
+
+typedef enum FptDiagnosticMode {
+    FPT_DIAGNOSTIC_DEPTH = 0,
+    FPT_DIAGNOSTIC_NORMAL = 1,
+    FPT_DIAGNOSTIC_MATERIAL = 2,
+    FPT_DIAGNOSTIC_HIT_MASK = 3,
+    FPT_DIAGNOSTIC_PATH_DIRECT = 4,
+    FPT_DIAGNOSTIC_PATH_ENVIRONMENT = 5,
+    FPT_DIAGNOSTIC_PATH_THROUGHPUT = 6,
+    FPT_DIAGNOSTIC_PATH_FINAL = 7,
+    FPT_DIAGNOSTIC_DIFFUSE_NORMAL = 8,
+    FPT_DIAGNOSTIC_MANDEL_COLOR_INDEX = 9,
+    FPT_DIAGNOSTIC_MANDEL_PALETTE_POSITION = 10,
+    FPT_DIAGNOSTIC_SDF_PRIMARY_STEPS = 11,
+    FPT_DIAGNOSTIC_SDF_SHADOW_STEPS = 12,
+    FPT_DIAGNOSTIC_SDF_NORMAL_EVALS = 13,
+    FPT_DIAGNOSTIC_SDF_BOUNCES = 14,
+    FPT_DIAGNOSTIC_SDF_BOUNCE_CONTRIBUTION = 15,
+} FptDiagnosticMode;
+
+struct FptDiagnosticConfig {
+    uint32_t mode;
+    uint32_t _pad0;
+    float max_distance;
+    float normal_mix;
+    uint32_t dispatch_origin[2];
+};
+
+struct FptMandelbulberFieldSample {
+    float distance;
+    float radius;
+    float derivative;
+    float iterations;
+};
+
+/* Replaces fpt_metal_render (src/metal_bridge.h:404-425; implementation
+ * src/metal_bridge.mm:4298-5863).  metallib_path, stitch_metallib_path,
+ * stitch_archive_path and shader_source are accepted and ignored (there is
+ * no Metal library to load); research statistics the CUDA path does not
+ * produce (bound-grid, stitch) are zero-filled.  Writes the presented 8-bit
+ * image as PNG to output_path (when non-NULL) and, when linear_output is
+ * non-NULL, the width*height*4 float accumulation buffer. */
+int fpt_metal_render(const char *metallib_path,
+                     const char *stitch_metallib_path,
+                     const char *stitch_archive_path,
+                     const char *output_path,
+                     const char *shader_source,
+                     size_t shader_source_len,
+                     const struct FptRenderConfig *config,
+                     double *build_ms,
+                     double *elapsed_ms,
+                     uint64_t *voxel_memory_bytes,
+                     uint32_t *voxel_active_bricks,
+                     uint64_t *voxel_active_cells,
+                     uint32_t *voxel_rejected_bricks,
+                     struct FptBoundGridStats *bound_grid_stats,
+                     uint32_t *stitch_cache_status,
+                     struct FptStitchValidationStats *stitch_validation_stats,
+                     struct FptStitchPipelineStats *stitch_pipeline_stats,
+                     struct FptSdfProfileStats *sdf_profile_stats,
+                     float *linear_output,
+                     size_t linear_output_len,
+                     char *error,
+                     size_t error_len);
+
+/* Replaces fpt_metal_diagnostic_render (src/metal_bridge.h:427-435;
+ * src/metal_bridge.mm:5865-6025).  Supported modes: depth, normal,
+ * hit mask, primary steps. */
+int fpt_metal_diagnostic_render(const char *metallib_path,
+                                const char *output_path,
+                                const char *shader_source,
+                                size_t shader_source_len,
+                                const struct FptRenderConfig *config,
+                                const struct FptDiagnosticConfig *diagnostic,
+                                double *elapsed_ms,
+                                char *error,
+                                size_t error_len);
+
+/* Replaces fpt_mandelbulber_sample_field (src/metal_bridge.h:437-446;
+ * src/metal_bridge.mm:4205-4296; kernel shaders/Shaders.metal:1001-1009):
+ * point_count xyzw points in, one {distance, radius, derivative, |iterations|}
+ * per point out. */
+int fpt_mandelbulber_sample_field(const char *metallib_path,
+                                  const char *shader_source,
+                                  size_t shader_source_len,
+                                  const struct FptRenderConfig *config,
+                                  const float *points_xyzw,
+                                  size_t point_count,
+                                  struct FptMandelbulberFieldSample *samples,
+                                  char *error,
+                                  size_t error_len);
+
+/* Host-only PNG comparison (src/metal_bridge.h:448-452;
+ * src/metal_bridge.mm:6062-6145): MAE, RMSE, 8x8 luminance SSIM,
+ * 64x64 low-frequency SSIM, written as JSON to report_path. */
+int fpt_compare_images(const char *baseline_path,
+                       const char *candidate_path,
+                       const char *report_path,
+                       char *error,
+                       size_t error_len);
+
+/* src/metal_bridge.h:454: device name, or returns 1 without a device. */
+int fpt_metal_device_name(char *name, size_t name_len);
+
+/* src/metal_bridge.h:456-458 (src/metal_bridge.mm:3715-3926): runs the
+ * voxel DDA / AABB / cell-ownership contract cases on the GPU and a 32^3
+ * sphere build both ways; 0 when every case holds. */
+int fpt_test_voxel_dda(const char *metallib_path, char *error, size_t error_len);
+
+/* src/metal_bridge.h:460-467: research JIT path; always returns 1 with
+ * "unsupported" (there is no runtime shader compiler here). */
+int fpt_test_async_stitch_context(const char *metallib_path,
+                                  const char *stitch_metallib_path,
+                                  const char *stitch_archive_path,
+                                  const struct FptRenderConfig *config,
+                                  struct FptAsyncJitStats *stats,
+                                  char *error,
+                                  size_t error_len);
+
+/* src/metal_bridge.h:469-474: field + gradient parity of the typed-program
+ * evaluator over 2^20 hash-seeded points (tolerances 2e-5*(1+|d|) and 1e-4,
+ * shaders/Shaders.metal:5106-5154). */
+int fpt_test_typed_soa(const char *metallib_path,
+                       const struct FptRenderConfig *config,
+                       struct FptStitchValidationStats *stats,
+                       char *error,
+                       size_t error_len);
+
+/* src/metal_bridge.h:476-486: interactive window; always returns 1 with
+ * "unsupported" (no window system on a headless GPU node). */
+int fpt_metal_preview(const char *metallib_path,
+                      const char *stitch_metallib_path,
+                      const char *const *stitch_archive_paths,
+                      const char *shader_source,
+                      size_t shader_source_len,
+                      const struct FptRenderConfig *config,
+                      const struct FptRenderConfig *scene_configs,
+                      uint32_t scene_config_count,
+                      uint32_t scene_config_index,
+                      char *error,
+                      size_t error_len);
+
+/* ------------------------------------------------------------------------- */
+/* Side entry points added by this library                                   */
+/* ------------------------------------------------------------------------- */
+
+/* Formula selected by FptCudaSceneExt.formula.  0 keeps the reference
+ * scene of FptRenderConfig.sdf_id.  2 and 8 follow Mandelbulber's formula
+ * numbering and the FP64 orbit code of src/mandelbulber/orbit.rs
+ * (mandelbulb 766-778, mandelbox 1636-1693, finalizers 638-683). */
+enum {
+    FPT_CUDA_FORMULA_REFERENCE = 0,
+    FPT_CUDA_FORMULA_MANDELBULB = 2,
+    FPT_CUDA_FORMULA_MANDELBOX = 8,
+    FPT_CUDA_FORMULA_MENGER_FOLD = 100,
+    FPT_CUDA_FORMULA_BULB_MENGER_HYBRID = 101,
+};
+
+enum { FPT_CUDA_RNG_HASH13 = 0, FPT_CUDA_RNG_PCG = 1 };
+enum { FPT_CUDA_BRDF_REFERENCE = 0, FPT_CUDA_BRDF_LAMBERT_GGX = 1 };
+enum { FPT_CUDA_NORMAL_CONFIG = 0, FPT_CUDA_NORMAL_ANALYTIC = 1 };
+enum { FPT_CUDA_SURROGATE_OFF = 0, FPT_CUDA_SURROGATE_SKIP = 1 };
+
+/* Scene features beyond FptRenderConfig.  A zero-initialised struct (or a
+ * NULL pointer) means the reference's semantics exactly. */
+struct FptCudaSceneExt {
+    uint32_t formula;            /* FPT_CUDA_FORMULA_* */
+    uint32_t iterations;         /* formula iterations (0: set_values[1] for Mandelbulber scenes) */
+    float bailout;               /* escape radius (0: set_values[2]) */
+    float power;                 /* Mandelbulb power */
+    float box_scale;             /* Mandelbox scale */
+    float box_min_radius;        /* Mandelbox minimum radius */
+    float box_fixed_radius;      /* Mandelbox fixed radius */
+    float box_fold_limit;        /* Mandelbox folding limit */
+    float box_fold_value;        /* Mandelbox folding value */
+    float menger_scale;          /* Menger fold scale */
+    uint32_t menger_iterations;  /* Menger fold iterations (hybrid: Menger slot every (period) steps) */
+    uint32_t hybrid_period;      /* hybrid schedule: bulb iterations per Menger iteration + 1 */
+    uint32_t ground_plane;       /* 1: union with the plane y = plane_height */
+    float plane_height;
+    uint32_t rng;                /* FPT_CUDA_RNG_* */
+    uint32_t seed;
+    uint32_t brdf;               /* FPT_CUDA_BRDF_* */
+    float albedo;                /* Lambert albedo of the fractal */
+    float ggx_alpha;             /* GGX roughness (alpha) of the fractal's specular lobe */
+    float specular_f0;           /* Schlick F0 of that lobe */
+    float plane_albedo;          /* Lambert albedo of the ground plane */
+    uint32_t normal_mode;        /* FPT_CUDA_NORMAL_* */
+    uint32_t sky_width;          /* equirect sky (RGB float, row 0 = +y pole); 0 = none */
+    uint32_t sky_height;
+    const float *sky_rgb;        /* host pointer, sky_width*sky_height*3 floats */
+    float sun_direction[3];      /* used with the equirect sky for sun NEE */
+    float sun_intensity;
+    uint32_t fp64_bisection;     /* 1: FP64 bisection at representable-position stops */
+    uint32_t surrogate;          /* FPT_CUDA_SURROGATE_* (needs a trained model) */
+    uint64_t surrogate_model;    /* handle from fpt_cuda_mlp_create */
+    float surrogate_margin;      /* exact-DE hand-over distance for surrogate skips */
+    float surrogate_safety;      /* step = safety * surrogate distance */
+    uint32_t _reserved[8];
+};
+
+/* Per-primary-ray output of fpt_cuda_trace_primary. */
+struct FptCudaPrimaryHit {
+    float distance;     /* travel from the camera to the hit (or to the stop point) */
+    float normal[3];    /* unit surface normal at the hit (0 on a miss) */
+    uint32_t steps;     /* distance-estimator evaluations of the march */
+    uint32_t hit;       /* 1 when the march converged on the surface */
+};
+
+/* Primary-ray march of every pixel (pixel-centre rays, no jitter, no DOF):
+ * the camera ray of shaders/Shaders.metal:5926-5956 marched with
+ * march / marchMandelbulber (3700-3783) and normalAt (3871-3971) or the
+ * analytic-derivative normal.  hits has width*height entries, row-major,
+ * row 0 at the bottom of the image (the accumulation layout). */
+int fpt_cuda_trace_primary(const struct FptRenderConfig *config,
+                           const struct FptCudaSceneExt *ext,
+                           struct FptCudaPrimaryHit *hits,
+                           size_t hit_count,
+                           double *elapsed_ms,
+                           char *error,
+                           size_t error_len);
+
+/* fpt_metal_render with a scene extension.  Same outputs; output_path may be
+ * NULL (no PNG).  Russian roulette, accumulation mode and chunking follow
+ * FptRenderConfig exactly. */
+int fpt_cuda_render(const struct FptRenderConfig *config,
+                    const struct FptCudaSceneExt *ext,
+                    const char *output_path,
+                    float *linear_output,
+                    size_t linear_output_len,
+                    uint8_t *rgba_output,
+                    size_t rgba_output_len,
+                    double *elapsed_ms,
+                    struct FptSdfProfileStats *profile,
+                    char *error,
+                    size_t error_len);
+
+/* Distance-estimator samples: xyz points (stride 4 floats) in, one
+ * {distance, orbit, derivative, iterations} per point out, evaluated by the
+ * scene's distance function (distanceSdf, shaders/Shaders.metal:3564-3610,
+ * or the extension formula).  gradients (optional, 3 floats per point) gets
+ * the analytic gradient when the scene has one. */
+int fpt_cuda_sample_distance(const struct FptRenderConfig *config,
+                             const struct FptCudaSceneExt *ext,
+                             const float *points_xyzw,
+                             size_t point_count,
+                             float *samples,
+                             float *gradients,
+                             char *error,
+                             size_t error_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FPT_CUDA_H */

@@ -1,0 +1,44 @@
+"""C ABI: struct layouts match the reference's pinned sizes and the library
+exports every entry point include/fpt_cuda.h declares (no GPU needed)."""
+import ctypes
+import os
+import re
+
+from fractalpathtracer_gb300 import ffi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_layout_sizes_match_reference():
+    # src/ffi.rs:494-507
+    assert ffi.layout_sizes() == ffi.REFERENCE_SIZES
+
+
+def test_field_offsets_match_reference_order():
+    c = ffi.FptRenderConfig
+    assert c.width.offset == 0 and c.sdf_chunk_samples.offset == 44
+    assert c.camera_position.offset == 60
+    # the typed SoA block closes the struct
+    assert c.sdf_typed_soa.offset + ctypes.sizeof(ffi.FptTypedSoAProgram) == 30448
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "fpt_cuda.h")).read()
+    return sorted(set(re.findall(r"^int\s+(fpt_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(native):
+    lib = native.lib()
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(native.EXPORTED) <= set(declared_symbols())
+
+
+def test_unsupported_entries_fail_cleanly_without_gpu(native):
+    import ctypes as C
+    lib = native.lib()
+    err = C.create_string_buffer(256)
+    assert lib.fpt_metal_preview(b"", b"", None, None, 0, None, None, 0, 0, err, len(err)) == 1
+    assert b"unsupported" in err.value
+    stats = ffi.FptAsyncJitStats()
+    assert lib.fpt_test_async_stitch_context(b"", b"", b"", None, C.byref(stats), err, len(err)) == 1
