@@ -59,8 +59,8 @@ def test_reference_scene_primary_matches_oracle(native):
     cfg = ffi.default_config()
     cfg.width, cfg.height = 96, 72
     cfg.sdf_id = ffi.SDF_MANDELBOX_FRACTAL
-    cfg.camera_position[:] = [0.0, 0.0, -6.0]
-    cfg.set_values[2] = -1.3
+    cfg.camera_position[:] = [0.5, 0.4, -4.5]
+    cfg.set_values[2] = -1.0
     gpu, _ = native.trace_primary(cfg, None)
     ref = oracle.trace_primary(cfg, None, fp64=True)
     agree, derr, ang, both = _compare(gpu, ref)
