@@ -344,14 +344,34 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     const bool batch = mode == FPT_SDF_ACCUMULATION_BATCH || (mode == FPT_SDF_ACCUMULATION_AUTO && auto_batch) || hydrated.preview;
     const bool chunked = !batch && (mode == FPT_SDF_ACCUMULATION_CHUNKED || mode == FPT_SDF_ACCUMULATION_AUTO);
     uint32_t step = batch ? spp : (chunked ? std::min(std::max(hydrated.sdf_chunk_samples, 1u), 64u) : 1u);
+    // Per-path colour scratch: launches of at most `sub` samples keep it
+    // under 2 GiB; the in-order reduction makes the split invisible.
+    const uint32_t sub_cap = uint32_t(std::max<size_t>(1, (size_t(2) << 30) / (pixels * sizeof(float4))));
+    if (!ensure_buffer((void **)&c.sample_rgb, &c.cap_sample_rgb, pixels * sizeof(float4) * std::min(step, sub_cap), error,
+                       error_len))
+        return 1;
     PathLaunch pl{};
-    pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height;
-    pl.accum = c.accum; pl.work_counter = c.counter; pl.grad_batch = c.grad_batch; pl.blocks = c.path_blocks;
+    pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height; pl.bounces = S.bounces;
+    pl.accum = c.accum; pl.counters = c.counter; pl.march_blocks = c.march_blocks;
     pl.profile = want_profile ? c.profile : nullptr;
+    {
+        // Wave scratch: path records and queues for up to wave_paths paths.
+        const size_t tiles = size_t((S.width + 7u) / 8u) * ((S.height + 3u) / 4u) * 32u;
+        size_t per_launch = tiles * std::min(step, sub_cap);
+        size_t cap = c.wave_paths ? c.wave_paths : (size_t(16) << 20);
+        cap = std::min(cap, per_launch);
+        pl.wave_paths = uint32_t(cap);
+        if (!ensure_buffer(&c.wave, &c.cap_wave, cap * kWaveBytesPerPath, error, error_len)) return 1;
+        pl.wave_scratch = c.wave;
+    }
+    pl.sample_rgb = c.sample_rgb;
     for (uint32_t start = 0; start < spp; start += step) {
-        pl.sample_begin = start;
-        pl.sample_end = std::min(spp, start + step);
-        if (!check(launch_pathtrace(pl, c.stream), "path-tracing launch", error, error_len)) return 1;
+        uint32_t end = std::min(spp, start + step);
+        for (uint32_t a = start; a < end; a += sub_cap) {
+            pl.sample_begin = a;
+            pl.sample_end = std::min(end, a + sub_cap);
+            if (!check(launch_pathtrace(pl, c.stream), "path-tracing launch", error, error_len)) return 1;
+        }
     }
     if (!check(launch_present(c.scene, S.width, S.height, c.accum, c.rgba, c.stream), "present launch", error, error_len)) return 1;
     cudaEventRecord(c.ev1, c.stream);

@@ -18,6 +18,8 @@ struct Context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     DeviceScene *scene = nullptr; size_t cap_scene = 0;
     float4 *accum = nullptr; size_t cap_accum = 0;
+    float4 *sample_rgb = nullptr; size_t cap_sample_rgb = 0;
+    void *wave = nullptr; size_t cap_wave = 0;
     uchar4 *rgba = nullptr; size_t cap_rgba = 0;
     unsigned int *counter = nullptr; size_t cap_counter = 0;
     unsigned long long *profile = nullptr; size_t cap_profile = 0;
@@ -27,8 +29,8 @@ struct Context {
     float4 *samples = nullptr; size_t cap_samples = 0;
     float *grads = nullptr; size_t cap_grads = 0;
     // launch tuning (set by the autotuner entry point; 0 = defaults)
-    uint32_t grad_batch = 0;
-    int path_blocks = 0;
+    uint32_t wave_paths = 0;   // paths per wave; 0 = min(all paths, 16M)
+    int march_blocks = 0;
 };
 
 Context &ctx();

@@ -7,15 +7,22 @@
 
 namespace fpt {
 
+// Bytes of wave scratch per path: path record (96), two march queues (8),
+// two shadow queues (128), shade queue (4).
+constexpr size_t kWaveBytesPerPath = 96 + 8 + 128 + 4;
+
 struct PathLaunch {
     const DeviceScene *scene;   // device pointer
     uint32_t kind;              // SceneKind
     uint32_t width, height;
+    uint32_t bounces;
     float4 *accum;              // width*height, running mean
-    unsigned int *work_counter; // device scratch word
+    float4 *sample_rgb;         // width*height*(sample_end-sample_begin) scratch: one colour per path
+    void *wave_scratch;         // wave_paths * kWaveBytesPerPath bytes
+    uint32_t wave_paths;        // paths per wave ("wavefront length")
+    unsigned int *counters;     // 8 device words
     uint32_t sample_begin, sample_end;
-    uint32_t grad_batch;        // 0 = default
-    int blocks;                 // persistent grid size, <= 0 = one wave of resident blocks
+    int march_blocks;           // persistent march grid, <= 0 = one wave of resident blocks
     unsigned long long *profile;  // 8 device counters or null
 };
 

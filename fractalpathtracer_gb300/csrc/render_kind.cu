@@ -2,6 +2,8 @@
 //
 // Compiled once per SceneKind with -DFPT_KIND=<n> so the six
 // specialisations build in parallel.
+#include <algorithm>
+
 #include "render_impl.cuh"
 
 #ifndef FPT_KIND
@@ -14,25 +16,54 @@ cudaError_t launch_pathtrace_kind(const PathLaunch &pl, cudaStream_t stream, int
 
 template <int KIND>
 static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
-    PathParams P;
-    P.scene = pl.scene; P.accum = pl.accum; P.work_counter = pl.work_counter;
-    P.tiles_x = (pl.width + 7u) / 8u;
-    uint32_t tiles_y = (pl.height + 3u) / 4u;
-    P.total_work = P.tiles_x * tiles_y * 32u;
-    P.sample_begin = pl.sample_begin; P.sample_end = pl.sample_end;
-    P.grad_batch = pl.grad_batch ? pl.grad_batch : 8u;
-    P.profile = pl.profile;
-    int blocks = pl.blocks;
-    if (blocks <= 0) {
-        int per_sm = 0, sms = 0, dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pathtrace_persistent<KIND>, 128, 0);
-        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    WaveParams W;
+    W.scene = pl.scene;
+    W.tiles_x = (pl.width + 7u) / 8u;
+    const uint32_t tiles_y = (pl.height + 3u) / 4u;
+    W.pixel_work = W.tiles_x * tiles_y * 32u;
+    W.sample_begin = pl.sample_begin;
+    W.sample_count = pl.sample_end - pl.sample_begin;
+    W.sample_rgb = pl.sample_rgb;
+    W.counters = pl.counters;
+    W.profile = pl.profile;
+    const uint32_t cap = pl.wave_paths;
+    char *base = static_cast<char *>(pl.wave_scratch);
+    W.paths = reinterpret_cast<PathRec *>(base);
+    W.q_shadow[0] = reinterpret_cast<ShadowJob *>(base + size_t(cap) * 96);
+    W.q_shadow[1] = W.q_shadow[0] + cap;
+    W.q_march[0] = reinterpret_cast<uint32_t *>(base + size_t(cap) * (96 + 128));
+    W.q_march[1] = W.q_march[0] + cap;
+    W.q_shade = W.q_march[1] + cap;
+    int sms = 0, dev = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int march_blocks = pl.march_blocks;
+    if (march_blocks <= 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<KIND>, 128, 0);
+        march_blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
-    cudaError_t e = cudaMemsetAsync(pl.work_counter, 0, sizeof(unsigned int), stream);
-    if (e != cudaSuccess) return e;
-    pathtrace_persistent<KIND><<<blocks, 128, 0, stream>>>(P);
+    int shade_per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_per_sm, shade_kernel<KIND>, 128, 0);
+    const int shade_blocks = sms * (shade_per_sm > 0 ? shade_per_sm : 1);
+    const uint64_t total = uint64_t(W.pixel_work) * W.sample_count;
+    cudaError_t e = cudaSuccess;
+    for (uint64_t wb = 0; wb < total; wb += cap) {
+        W.wave_base = uint32_t(wb);
+        W.n_paths = uint32_t(std::min<uint64_t>(cap, total - wb));
+        if ((e = cudaMemsetAsync(W.counters, 0, C_COUNT * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+        camera_kernel<<<std::min<uint32_t>((W.n_paths + 255u) / 256u, uint32_t(sms) * 16u), 256, 0, stream>>>(W);
+        for (uint32_t b = 0; b <= pl.bounces; ++b) {
+            const int cur = int(b & 1u);
+            reset_counters_kernel<<<1, 32, 0, stream>>>(W.counters, cur ^ 1);
+            march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
+            if (b < pl.bounces) shade_kernel<KIND><<<shade_blocks, 128, 0, stream>>>(W, cur);
+        }
+        finalize_kernel<<<(W.n_paths + 255u) / 256u, 256, 0, stream>>>(W);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const uint32_t pixels = pl.width * pl.height;
+    reduce_samples_kernel<<<(pixels + 255u) / 256u, 256, 0, stream>>>(pl.sample_rgb, pl.accum, pixels, pl.sample_begin,
+                                                                       W.sample_count);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,496 @@
+// wavefront.cuh -- wavefront path tracer: persistent march kernel + shade kernel.
+//
+// renderPath (shaders/Shaders.metal:5926-6026) is split at its marches.  A
+// wave of paths (pixel, sample) lives in device memory as PathRec records;
+// work moves through queues of path indices:
+//
+//   camera_kernel   writes every path's camera ray into the march queue
+//   march_kernel    persistent: each lane takes one march job (a path ray or
+//                   a sun shadow ray) from the queue, marches it with one
+//                   distance evaluation per loop iteration, and on finishing
+//                   takes the next job at once (per-lane regeneration, one
+//                   warp-aggregated atomic per refill); hits go to the shade
+//                   queue, misses add the environment
+//   shade_kernel    material, normal, sun shadow ray, scatter and Russian
+//                   roulette of every hit; continuing paths go back to the
+//                   march queue
+//   finalize_kernel combines each path's light into its sample colour
+//
+// The sun term of a bounce only adds light (the scatter does not depend on
+// it), so shadow rays of bounce b march in the same pass as the path rays of
+// bounce b+1.  Random numbers are keyed by (pixel, sample, bounce), so the
+// order in which work is scheduled never changes a path.
+#pragma once
+
+#include "fpt_march.cuh"
+#include "fpt_kernels.h"
+
+namespace fpt {
+
+enum PathFlags : uint32_t { PF_DONE = 1u << 8, PF_INVISIBLE = 1u << 9, PF_VALID = 1u << 10 };
+
+struct alignas(16) PathRec {
+    float4 pos;     // xyz march origin or hit point, w side
+    float4 dir;     // xyz direction, w sky mask
+    float4 color;   // xyz throughput, w state bits (bounce | flags)
+    float4 light;   // xyz emission + environment light, w slot bits
+    float4 shadow;  // xyz sun light from shadow rays
+    float4 grad;    // xyz background gradient colour of the camera ray
+};
+
+struct alignas(16) ShadowJob {
+    float4 origin;  // xyz hit point, w path index bits
+    float4 normal;  // xyz normal the ray leaves along (offset 0.001)
+    float4 dir;     // xyz light direction
+    float4 contrib; // xyz light added when the ray escapes
+};
+
+// Device counters of one wave.
+enum Counter : uint32_t { C_MARCH0 = 0, C_MARCH1 = 1, C_SHADOW0 = 2, C_SHADOW1 = 3, C_SHADE = 4, C_HEAD = 5, C_COUNT = 8 };
+
+struct WaveParams {
+    const DeviceScene *scene;
+    PathRec *paths;
+    uint32_t *q_march[2];
+    ShadowJob *q_shadow[2];
+    uint32_t *q_shade;
+    uint32_t *counters;
+    float4 *sample_rgb;
+    uint32_t wave_base;        // first work index of this wave
+    uint32_t n_paths;          // paths in this wave
+    uint32_t pixel_work;       // tiles * 32
+    uint32_t tiles_x;
+    uint32_t sample_begin, sample_count;
+    unsigned long long *profile;   // 8 counters or null
+};
+
+__device__ __forceinline__ uint32_t fbits(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ float bitsf(uint32_t v) { return __uint_as_float(v); }
+
+// Warp-aggregated append: one atomic per warp for all participating lanes.
+__device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
+    unsigned mask = __activemask();
+    unsigned bal = __ballot_sync(mask, want);
+    if (!want) return 0xffffffffu;
+    uint32_t lane = threadIdx.x & 31u;
+    uint32_t leader = __ffs(bal) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(bal));
+    base = __shfl_sync(bal, base, leader);
+    return base + __popc(bal & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void wave_pixel(const WaveParams &W, uint32_t path, uint32_t width, uint32_t height, uint32_t &px,
+                                           uint32_t &py, uint32_t &s_rel, bool &valid) {
+    uint32_t g = W.wave_base + path;
+    s_rel = g / W.pixel_work;
+    uint32_t idx = g - s_rel * W.pixel_work;
+    uint32_t tile = idx >> 5, within = idx & 31u;
+    uint32_t tx = tile % W.tiles_x, ty = tile / W.tiles_x;
+    px = tx * 8u + (within & 7u);
+    py = ty * 4u + (within >> 3);
+    valid = px < width && py < height;
+}
+
+__device__ __forceinline__ PathRng path_rng(const DeviceScene &S, uint32_t pixel, uint32_t sample) {
+    PathRng r;
+    uint32_t px = pixel % S.width, py = pixel / S.width;
+    float2 uv = screen_uv(px, py, S);
+    r.init(S.rng == FPT_CUDA_RNG_PCG, S.seed, pixel, sample, uv.x, uv.y);
+    return r;
+}
+
+// ---------------------------------------------------------------- camera
+static __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
+    const DeviceScene &S = *W.scene;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p - threadIdx.x < W.n_paths; p += gridDim.x * blockDim.x) {
+        bool in_wave = p < W.n_paths;
+        uint32_t px = 0, py = 0, s_rel = 0;
+        bool valid = false;
+        if (in_wave) wave_pixel(W, p, S.width, S.height, px, py, s_rel, valid);
+        bool march = false;
+        if (valid) {
+            uint32_t pixel = py * S.width + px;
+            uint32_t sample = W.sample_begin + s_rel;
+            float2 uv = screen_uv(px, py, S);
+            PathRng rng;
+            rng.init(S.rng == FPT_CUDA_RNG_PCG, S.seed, pixel, sample, uv.x, uv.y);
+            float3 rp, dr;
+            PathRec R;
+            uint32_t slot = pixel * W.sample_count + s_rel;
+            R.light = make_float4(0.f, 0.f, 0.f, bitsf(slot));
+            R.shadow = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!camera_ray(S, uv, rng, true, rp, dr)) {
+                R.color = make_float4(0.f, 0.f, 0.f, bitsf(PF_VALID | PF_DONE | PF_INVISIBLE));
+                R.pos = make_float4(0.f, 0.f, 0.f, 1.f);
+                R.dir = make_float4(0.f, 0.f, 1.f, 0.f);
+                R.grad = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                bool done = S.bounces == 0u;
+                R.pos = make_float4(rp.x, rp.y, rp.z, 1.0f);
+                R.dir = make_float4(dr.x, dr.y, dr.z, 0.0f);
+                R.color = make_float4(1.f, 1.f, 1.f, bitsf(PF_VALID | (done ? PF_DONE : 0u)));
+                float3 g = background_gradient(dr, S);
+                R.grad = make_float4(g.x, g.y, g.z, 0.f);
+                march = !done;
+            }
+            W.paths[p] = R;
+        } else if (in_wave) {
+            W.paths[p].color = make_float4(0.f, 0.f, 0.f, 0.f);   // not a pixel of the image
+        }
+        uint32_t at = warp_append(&W.counters[C_MARCH0], march);
+        if (march) W.q_march[0][at] = p;
+    }
+}
+
+// ---------------------------------------------------------------- march
+struct MarchJob {
+    uint32_t path;      // path index
+    uint32_t bounce;
+    bool shadow;
+    float4 contrib;     // shadow: light to add when unoccluded
+    float3 rp0;         // shadow: hit point the ray leaves
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
+    const DeviceScene &S = *W.scene;
+    TranslucencyProbe<KIND> probe{W.scene};
+    const uint32_t n_path = W.counters[C_MARCH0 + cur];
+    const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
+    const uint32_t *qm = W.q_march[cur];
+    const ShadowJob *qs = W.q_shadow[cur];
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned FULL = 0xffffffffu;
+    const float3 cam = mk3(S.cam_pos[0], S.cam_pos[1], S.cam_pos[2]);
+    March m;
+    MarchJob job;
+    bool active = false, pending = false, retired = false;
+    uint32_t c_primary = 0, c_secondary = 0, c_shadow = 0, c_paths = 0;
+    while (true) {
+        // Refill every lane whose march finished: one atomic per warp.
+        unsigned need = __ballot_sync(FULL, !active && !pending && !retired);
+        if (need) {
+            uint32_t leader = __ffs(need) - 1, base = 0;
+            if (lane == leader) base = atomicAdd(&W.counters[C_HEAD], (unsigned)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (!active && !pending && !retired) {
+                uint32_t idx = base + __popc(need & ((1u << lane) - 1u));
+                if (idx >= total) {
+                    retired = true;
+                } else if (idx < n_path) {
+                    job.path = qm[idx];
+                    job.shadow = false;
+                    const PathRec &R = W.paths[job.path];
+                    float4 pos = R.pos, dir = R.dir;
+                    job.bounce = fbits(R.color.w) & 0xffu;
+                    int ni = job.bounce == 0u ? int(S.render[1]) : int(S.render[1] / (S.render[5] * 2.0f + 1.0f));
+                    active = march_begin(m, S, mk3(pos.x, pos.y, pos.z), mk3(dir.x, dir.y, dir.z), ni, S.render[3], 0.0002f);
+                    pending = !active;
+                } else {
+                    const ShadowJob &J = qs[idx - n_path];
+                    float4 o = J.origin, nn = J.normal, d = J.dir;
+                    job.path = fbits(o.w);
+                    job.shadow = true;
+                    job.contrib = J.contrib;
+                    job.rp0 = mk3(o.x, o.y, o.z);
+                    float3 start = job.rp0 + mk3(nn.x, nn.y, nn.z) * 0.001f;
+                    active = march_begin(m, S, start, mk3(d.x, d.y, d.z), int(S.render[1]), S.render[3], 0.0002f);
+                    pending = !active;
+                }
+            }
+        }
+        if (!__any_sync(FULL, !retired)) break;
+        // One distance evaluation for every lane with a march in flight.
+        if (active) {
+            float d = scene_eval<KIND>(S, m.pos, EV_MAP).d;
+            active = march_update(m, S, d, probe);
+            pending = !active;
+        }
+        if (pending) {
+            pending = false;
+            if (job.shadow) {
+                c_shadow += m.steps;
+                if (len3(job.rp0 - m.pos) > S.render[4] * 0.99f) {
+                    float4 &sh = W.paths[job.path].shadow;
+                    sh = make_float4(sh.x + job.contrib.x, sh.y + job.contrib.y, sh.z + job.contrib.z, sh.w);
+                }
+            } else {
+                if (job.bounce == 0u) c_primary += m.steps; else c_secondary += m.steps;
+                PathRec &R = W.paths[job.path];
+                float3 r = m.pos - cam;
+                float travel2 = dot(r, r);
+                float maxd = S.render[4], far = maxd * 0.99f;
+                bool hit = !(travel2 > far * far);
+                if (job.bounce == 0u && travel2 > maxd * maxd) R.dir.w = 1.0f;
+                if (!hit) {
+                    float4 dir = R.dir;
+                    float3 env = environment(mk3(dir.x, dir.y, dir.z), S);
+                    float4 col = R.color, li = R.light;
+                    if (S.brdf == FPT_CUDA_BRDF_LAMBERT_GGX) env = env * mk3(col.x, col.y, col.z);
+                    R.light = make_float4(li.x + env.x, li.y + env.y, li.z + env.z, li.w);
+                    R.color.w = bitsf(fbits(col.w) | PF_DONE);
+                    c_paths += 1;
+                } else {
+                    R.pos = make_float4(m.pos.x, m.pos.y, m.pos.z, R.pos.w);
+                }
+                uint32_t at = warp_append(&W.counters[C_SHADE], hit);
+                if (hit) W.q_shade[at] = job.path;
+            }
+        }
+    }
+    if (W.profile) {
+        uint32_t v[4] = {c_primary, c_secondary, c_shadow, c_paths};
+        const int slot[4] = {0, 1, 2, 5};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            uint32_t s = v[k];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+            if (lane == 0 && s) atomicAdd(W.profile + slot[k], (unsigned long long)s);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- shade
+// Lambert + GGX lobe (Heitz 2014 height-correlated Smith masking, Schlick
+// Fresnel): f_cos = BRDF * cos(theta_l) and the pdf of the 1/2-1/2 mixture.
+__device__ __forceinline__ void ggx_eval(const DeviceScene &S, float3 n, float3 v, float3 l, float albedo, bool plane,
+                                         float3 &f_cos, float &pdf) {
+    float nl = dot(n, l), nv = dot(n, v);
+    if (nl <= 0.0f || nv <= 0.0f) { f_cos = mk3(0.0f); pdf = 0.0f; return; }
+    float diffuse = albedo * (1.0f / kPi);
+    if (plane) { f_cos = mk3(diffuse * nl); pdf = nl * (1.0f / kPi); return; }
+    float a = S.ggx_alpha, a2 = a * a;
+    float3 h = normalize3(v + l);
+    float nh = dot(n, h);
+    float dd = nh * nh * (a2 - 1.0f) + 1.0f;
+    float D = a2 / (kPi * dd * dd);
+    float tv = fmaxf(1.0f - nv * nv, 0.0f) / fmaxf(nv * nv, 1e-12f);
+    float tl = fmaxf(1.0f - nl * nl, 0.0f) / fmaxf(nl * nl, 1e-12f);
+    float lv = (sqrtf(1.0f + a2 * tv) - 1.0f) * 0.5f, ll = (sqrtf(1.0f + a2 * tl) - 1.0f) * 0.5f;
+    float G = 1.0f / (1.0f + lv + ll);
+    float F = S.specular_f0 + (1.0f - S.specular_f0) * pow5f(1.0f - fmaxf(dot(v, h), 0.0f));
+    float spec = D * G * F / (4.0f * nv * nl);
+    f_cos = mk3((diffuse * (1.0f - F) + spec) * nl);
+    pdf = 0.5f * nl * (1.0f / kPi) + 0.5f * (1.0f / (1.0f + lv)) * D / (4.0f * nv);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
+    const DeviceScene &S = *W.scene;
+    const int next = cur ^ 1;
+    const uint32_t n = W.counters[C_SHADE];
+    const bool ggx = S.brdf == FPT_CUDA_BRDF_LAMBERT_GGX;
+    uint32_t c_normal = 0, c_material = 0, c_paths = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += gridDim.x * blockDim.x) {
+        bool live = i < n;
+        bool emit_march = false, emit_shadow = false;
+        uint32_t path = 0;
+        ShadowJob J;
+        if (live) {
+            path = W.q_shade[i];
+            PathRec R = W.paths[path];
+            uint32_t state = fbits(R.color.w);
+            const int bounce = int(state & 0xffu);
+            const uint32_t slot = fbits(R.light.w);
+            const uint32_t s_rel = slot % W.sample_count, pixel = slot / W.sample_count;
+            PathRng rng = path_rng(S, pixel, W.sample_begin + s_rel);
+            float3 hit = mk3(R.pos.x, R.pos.y, R.pos.z), dr = mk3(R.dir.x, R.dir.y, R.dir.z);
+            float3 color = mk3(R.color.x, R.color.y, R.color.z), light = mk3(R.light.x, R.light.y, R.light.z);
+            float side = R.pos.w;
+            // Material and normal (userSdf + normalAt, shaders/Shaders.metal:5980-5982).
+            Material mt;
+            float3 nrm;
+            c_material += 1;
+            if (S.formula != 0 && S.ext_normal == FPT_CUDA_NORMAL_ANALYTIC && S.fractal_style_mode == 0u && ggx) {
+                // One dual-number evaluation gives the surface id and the gradient.
+                float3 g;
+                analytic_gradient<KIND>(S, hit, g);
+                int surface = 0;
+                if (S.ground_plane) {
+                    Eval e = ext_eval<KIND>(S, hit);
+                    surface = e.id;
+                }
+                mt = default_material();
+                mt.rgb = mk3(surface ? S.plane_albedo : S.albedo);
+                mt.surface = surface;
+                nrm = (finite3(g) && dot(g, g) > 0.0f) ? normalize3(g) : mk3(0.f, 1.f, 0.f);
+                c_normal += 1;
+            } else {
+                mt = material_of(S, scene_eval<KIND>(S, hit, EV_MATERIAL));
+                nrm = normal_direct<KIND>(hit, S);
+                c_normal += normal_is_analytic(S) ? 1u : uint32_t(tap_count(S));
+            }
+            if (mt.emission > 0.001f) light = light + (ggx ? mt.rgb * (mt.emission) * color : mt.rgb * mt.emission);
+            if (ggx && dot(nrm, dr) > 0.0f) nrm = -nrm;
+            // Sun: direction with divergence, shadow ray (shaders/Shaders.metal:5846-5861).
+            bool sun = S.sun[0] == 1.0f || (ggx && S.sun_power > 0.0f);
+            if (sun) {
+                float3 ld = mk3(S.sun_dir[0], S.sun_dir[1], S.sun_dir[2]);
+                float h1 = rng.uniform(SLOT_SUN0, bounce), h2 = rng.uniform(SLOT_SUN1, bounce);
+                float sa, ca;
+                sincosf(h1 * 2.0f * kPi, &sa, &ca);
+                float s = sqrtf(h2) * S.sun[4];
+                ld = rotate_camera(ld, ca * s, sa * s);
+                float3 contrib;
+                float3 sc = mk3(S.sun_color[0], S.sun_color[1], S.sun_color[2]);
+                if (ggx) {
+                    float3 fc; float pdf;
+                    ggx_eval(S, nrm, -dr, ld, mt.rgb.x, mt.surface == 1, fc, pdf);
+                    float power = S.sun_power > 0.0f ? S.sun_power : S.sun[3];
+                    contrib = fc * color * sc * power;
+                    emit_shadow = dot(ld, nrm) > 0.0f;
+                } else {
+                    contrib = sc * (S.sun[3] * fmaxf(dot(nrm, ld), 0.0f) * mt.roughness * (1.0f - mt.translucency));
+                    emit_shadow = true;
+                }
+                J.origin = make_float4(hit.x, hit.y, hit.z, bitsf(path));
+                J.normal = make_float4(nrm.x, nrm.y, nrm.z, 0.f);
+                J.dir = make_float4(ld.x, ld.y, ld.z, 0.f);
+                J.contrib = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+            }
+            // Scatter.
+            bool terminate = false;
+            if (ggx) {
+                float3 v = -dr;
+                float sgn = nrm.z >= 0.0f ? 1.0f : -1.0f;   // basis: Duff et al., JCGT 2017
+                float aa = -1.0f / (sgn + nrm.z);
+                float bb = nrm.x * nrm.y * aa;
+                float3 t = mk3(1.0f + sgn * nrm.x * nrm.x * aa, sgn * bb, -sgn * nrm.x);
+                float3 b = mk3(bb, sgn + nrm.y * nrm.y * aa, -nrm.y);
+                float u1 = rng.uniform(SLOT_DIR0, bounce), u2 = rng.uniform(SLOT_DIR1, bounce);
+                float3 l;
+                if (mt.surface == 1 || rng.uniform(SLOT_LOBE, bounce) < 0.5f) {
+                    float r = sqrtf(u1), sp, cp;
+                    sincosf(2.0f * kPi * u2, &sp, &cp);
+                    l = t * (r * cp) + b * (r * sp) + nrm * sqrtf(fmaxf(0.0f, 1.0f - u1));
+                } else {
+                    // Visible-normal sampling (Heitz, JCGT 2018).
+                    float a = S.ggx_alpha;
+                    float3 vl = mk3(dot(v, t), dot(v, b), dot(v, nrm));
+                    float3 vh = normalize3(mk3(a * vl.x, a * vl.y, vl.z));
+                    float lensq = vh.x * vh.x + vh.y * vh.y;
+                    float3 t1 = lensq > 0.0f ? mk3(-vh.y, vh.x, 0.0f) * rsqrtf(lensq) : mk3(1.f, 0.f, 0.f);
+                    float3 t2 = cross3(vh, t1);
+                    float r = sqrtf(u1), sp, cp;
+                    sincosf(2.0f * kPi * u2, &sp, &cp);
+                    float p1 = r * cp, p2 = r * sp;
+                    float sm = 0.5f * (1.0f + vh.z);
+                    p2 = (1.0f - sm) * sqrtf(fmaxf(1.0f - p1 * p1, 0.0f)) + sm * p2;
+                    float3 nh = t1 * p1 + t2 * p2 + vh * sqrtf(fmaxf(0.0f, 1.0f - p1 * p1 - p2 * p2));
+                    float3 hl = normalize3(mk3(a * nh.x, a * nh.y, fmaxf(0.0f, nh.z)));
+                    float3 h = t * hl.x + b * hl.y + nrm * hl.z;
+                    l = reflect3(-v, h);
+                }
+                float3 fc; float pdf;
+                ggx_eval(S, nrm, v, l, mt.rgb.x, mt.surface == 1, fc, pdf);
+                if (!(pdf > 0.0f)) terminate = true;
+                else {
+                    color = color * (fc / pdf);
+                    dr = normalize3(l);
+                    hit = hit + nrm * (0.001f * signf(dot(dr, nrm)));
+                }
+            } else {
+                float r1 = rng.uniform(SLOT_SCATTER, bounce), r2 = rng.uniform(SLOT_FRESNEL, bounce);
+                float3 nn = nrm;
+                if (r1 > mt.translucency) {
+                    float3 metal = reflect3(dr, nn);
+                    float h1 = rng.uniform(SLOT_DIR0, bounce), h2 = rng.uniform(SLOT_DIR1, bounce);   // randomVector :557-569
+                    float3 nz = normalize3(nn);
+                    float3 uu = normalize3(cross3(nz, mk3(0.0f, 1.0f, 1.0f)));
+                    float3 vv = cross3(uu, nz);
+                    float ra = sqrtf(h2), sr, cr;
+                    sincosf(kPi * 2.0f * h1, &sr, &cr);
+                    float3 diffuse = normalize3(uu * (ra * cr) + vv * (ra * sr) + nz * sqrtf(fmaxf(1.0f - h2, 0.0f)));
+                    float f0 = (mt.ior - 1.0f) / (mt.ior + 1.0f);
+                    f0 = f0 * f0;
+                    float ct = clampf(dot(nn, -dr), 0.0f, 1.0f);
+                    float fres = f0 + (1.0f - f0) * pow5f(1.0f - ct);
+                    float3 ndir = normalize3(mix3(metal, diffuse, mt.roughness));
+                    if (r2 < fres * mt.specular) ndir = metal;
+                    else color = color * mt.rgb;
+                    dr = ndir;
+                } else {
+                    float eta = side == 1.0f ? 1.0f / mt.ior : mt.ior;
+                    if (side != 1.0f) nn = -nn;
+                    float f0 = (mt.ior - 1.0f) / (mt.ior + 1.0f);
+                    f0 = f0 * f0;
+                    float ct = clampf(dot(nn, -dr), 0.0f, 1.0f);
+                    float fres = f0 + (1.0f - f0) * pow5f(1.0f - ct);
+                    float3 refr = refract3(dr, nn, eta);
+                    float3 refl = reflect3(dr, nn);
+                    if (dot(refr, refr) < 0.000001f || !isfinite(refr.x) || r2 < fres) {
+                        dr = normalize3(refl);
+                    } else {
+                        dr = normalize3(refr);
+                        side *= -1.0f;
+                        color = color * (mix3(mk3(1.0f), mt.rgb, 0.35f) * (1.0f - fres * 0.5f));
+                    }
+                }
+                hit = hit + nn * (0.001f * signf(dot(dr, nn)));
+            }
+            // Russian roulette (shaders/Shaders.metal:6016-6021).
+            if (!terminate && S.russian_roulette != 0u && bounce + 1 < int(S.bounces) && float(bounce + 1) >= S.rr_start) {
+                float surv = clampf(maxc3(color), clampf(S.rr_min_prob, 0.01f, 1.0f), 1.0f);
+                if (rng.uniform(SLOT_RR, bounce) > surv) terminate = true;
+                else color = color / surv;
+            }
+            if (!terminate && bounce + 1 >= int(S.bounces)) terminate = true;
+            emit_march = !terminate;
+            uint32_t nstate = (state & ~0xffu) | uint32_t(bounce + 1) | (terminate ? PF_DONE : 0u);
+            if (terminate) c_paths += 1;
+            R.pos = make_float4(hit.x, hit.y, hit.z, side);
+            R.dir = make_float4(dr.x, dr.y, dr.z, R.dir.w);
+            R.color = make_float4(color.x, color.y, color.z, bitsf(nstate));
+            R.light = make_float4(light.x, light.y, light.z, R.light.w);
+            W.paths[path] = R;
+        }
+        uint32_t at = warp_append(&W.counters[C_MARCH0 + next], emit_march);
+        if (emit_march) W.q_march[next][at] = path;
+        uint32_t sat = warp_append(&W.counters[C_SHADOW0 + next], emit_shadow);
+        if (emit_shadow) W.q_shadow[next][sat] = J;
+    }
+    if (W.profile) {
+        uint32_t v[3] = {c_normal, c_material, c_paths};
+        const int slot[3] = {3, 7, 5};
+        const unsigned FULL = 0xffffffffu;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            uint32_t s = v[k];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+            if ((threadIdx.x & 31u) == 0 && s) atomicAdd(W.profile + slot[k], (unsigned long long)s);
+        }
+    }
+}
+
+// Resets the counters the next pass appends to.
+static __global__ void reset_counters_kernel(uint32_t *counters, int next) {
+    if (threadIdx.x == 0) {
+        counters[C_MARCH0 + next] = 0u;
+        counters[C_SHADOW0 + next] = 0u;
+        counters[C_SHADE] = 0u;
+        counters[C_HEAD] = 0u;
+    }
+}
+
+// Path colour: (light + sun light) times throughput (reference estimator)
+// or the throughput-weighted sum (extension estimator), gradient mix and
+// the 8.0 clamp of renderPath (shaders/Shaders.metal:6023-6025).
+static __global__ void __launch_bounds__(256) finalize_kernel(WaveParams W) {
+    const DeviceScene &S = *W.scene;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= W.n_paths) return;
+    const PathRec &R = W.paths[p];
+    uint32_t state = fbits(R.color.w);
+    if (!(state & PF_VALID)) return;
+    float3 col = mk3(0.0f);
+    if (!(state & PF_INVISIBLE)) {
+        float3 light = mk3(R.light.x + R.shadow.x, R.light.y + R.shadow.y, R.light.z + R.shadow.z);
+        col = S.brdf == FPT_CUDA_BRDF_LAMBERT_GGX ? light : light * mk3(R.color.x, R.color.y, R.color.z);
+        if (S.world[6] == 1.0f) col = mix3(col, mk3(R.grad.x, R.grad.y, R.grad.z), R.dir.w);
+        col = min3(col, mk3(8.0f));
+    }
+    W.sample_rgb[fbits(R.light.w)] = make_float4(col.x, col.y, col.z, 1.0f);
+}
+
+}  // namespace fpt
