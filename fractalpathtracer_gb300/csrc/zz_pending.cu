@@ -1,10 +1,8 @@
 #include "bridge_internal.h"
 namespace fpt {
-int voxel_render_core(const FptRenderConfig &, const FptCudaSceneExt *, DeviceScene &, const char *, float *, uint8_t *, double *, uint64_t *, uint32_t *, uint64_t *, double *, char *error, size_t error_len) { set_error(error, error_len, "voxel: not built"); return 1; }
 bool surrogate_bind(uint64_t, DeviceScene &, char *error, size_t error_len) { set_error(error, error_len, "surrogate: not built"); return false; }
 }
 extern "C" {
 int fpt_metal_diagnostic_render(const char *, const char *, const char *, size_t, const struct FptRenderConfig *, const struct FptDiagnosticConfig *, double *, char *error, size_t error_len) { fpt::set_error(error, error_len, "diagnostic: not built"); return 1; }
-int fpt_test_voxel_dda(const char *, char *error, size_t error_len) { fpt::set_error(error, error_len, "voxel: not built"); return 1; }
 int fpt_test_typed_soa(const char *, const struct FptRenderConfig *, struct FptStitchValidationStats *, char *error, size_t error_len) { fpt::set_error(error, error_len, "typed soa: not built"); return 1; }
 }

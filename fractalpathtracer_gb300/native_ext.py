@@ -1,9 +1,100 @@
-"""ctypes declarations of the side entry points added after the base set (voxel, MLP, batch)."""
+"""ctypes declarations and wrappers of the side entry points (voxel, MLP, batch)."""
 from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
+
+from . import ffi
+
+
+class FptCudaVoxelInfo(C.Structure):
+    _fields_ = [("resolution", C.c_uint32), ("brick_size", C.c_uint32), ("brick_grid", C.c_uint32),
+                ("active_bricks", C.c_uint32), ("active_cells", C.c_uint64), ("memory_bytes", C.c_uint64),
+                ("build_ms", C.c_double)]
+
+
+class FptCudaVoxelHit(C.Structure):
+    _fields_ = [("t", C.c_float), ("cell", C.c_uint32), ("normal_axis", C.c_uint32), ("steps", C.c_uint32),
+                ("shadow_steps", C.c_uint32), ("lit", C.c_uint32)]
+
+
+VOXEL_HIT_DTYPE = np.dtype([("t", np.float32), ("cell", np.uint32), ("normal_axis", np.uint32), ("steps", np.uint32),
+                            ("shadow_steps", np.uint32), ("lit", np.uint32)])
+
 
 def declare(L: C.CDLL) -> None:
-    """Declares argtypes for optional entry points present in this build."""
-    return None
+    P = C.POINTER
+    cfg, ext = P(ffi.FptRenderConfig), P(ffi.FptCudaSceneExt)
+    err = [C.c_char_p, C.c_size_t]
+    L.fpt_cuda_voxel_build.argtypes = [cfg, ext, C.c_uint32, P(FptCudaVoxelInfo)] + err
+    L.fpt_cuda_voxel_read.argtypes = [P(C.c_uint32), C.c_size_t, P(C.c_uint8), P(C.c_uint16), P(C.c_uint32), C.c_size_t] + err
+    L.fpt_cuda_dda_sequence.argtypes = [P(C.c_float), C.c_size_t, C.c_uint32, P(C.c_uint32), P(C.c_uint32),
+                                        P(FptCudaVoxelHit)] + err
+    L.fpt_cuda_voxel_render.argtypes = [cfg, ext, P(FptCudaVoxelHit), C.c_size_t, P(C.c_uint8), C.c_size_t,
+                                        P(C.c_double)] + err
+    for name in ("fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render"):
+        getattr(L, name).restype = C.c_int
+
+
+def _err():
+    return C.create_string_buffer(1024)
+
+
+def _check(rc, e):
+    from .native import NativeError
+    if rc != 0:
+        raise NativeError(e.value.decode("utf-8", "replace"))
+
+
+def voxel_build(cfg, ext, brick_size: int = 8) -> dict:
+    from .native import lib
+    info = FptCudaVoxelInfo()
+    e = _err()
+    _check(lib().fpt_cuda_voxel_build(C.byref(cfg), C.byref(ext) if ext is not None else None, brick_size, C.byref(info), e,
+                                      len(e)), e)
+    return {k: getattr(info, k) for k, _ in FptCudaVoxelInfo._fields_}
+
+
+def voxel_read(info: dict, table=True, occupancy=True, distance=True, cells=False):
+    from .native import lib
+    nb = info["brick_grid"] ** 3
+    bvol = info["brick_size"] ** 3 if info["brick_size"] else 1
+    ncell = info["active_bricks"] * bvol if info["brick_size"] else info["resolution"] ** 3
+    t = np.zeros(max(nb, 1), np.uint32) if table else None
+    o = np.zeros(max(ncell, 1), np.uint8) if occupancy else None
+    d = np.zeros(max(ncell, 1), np.uint16) if distance else None
+    c = np.zeros((max(ncell, 1), 3), np.uint32) if cells else None
+    e = _err()
+    p = lambda a, ty: a.ctypes.data_as(C.POINTER(ty)) if a is not None else None
+    _check(lib().fpt_cuda_voxel_read(p(t, C.c_uint32), nb, p(o, C.c_uint8), p(d, C.c_uint16), p(c, C.c_uint32), ncell, e, len(e)), e)
+    return t, o, d, c
+
+
+def dda_sequence(rays: np.ndarray, capacity: int = 0):
+    from .native import lib
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    n = len(r)
+    hits = np.zeros(n, VOXEL_HIT_DTYPE)
+    seq = np.zeros((n, capacity), np.uint32) if capacity else None
+    seq_len = np.zeros(n, np.uint32) if capacity else None
+    e = _err()
+    _check(lib().fpt_cuda_dda_sequence(r.ctypes.data_as(C.POINTER(C.c_float)), n, capacity,
+                                       seq.ctypes.data_as(C.POINTER(C.c_uint32)) if seq is not None else None,
+                                       seq_len.ctypes.data_as(C.POINTER(C.c_uint32)) if seq_len is not None else None,
+                                       hits.ctypes.data_as(C.POINTER(FptCudaVoxelHit)), e, len(e)), e)
+    return hits, seq, seq_len
+
+
+def voxel_render(cfg, ext=None, image=True):
+    from .native import lib
+    n = cfg.width * cfg.height
+    hits = np.zeros(n, VOXEL_HIT_DTYPE)
+    rgba = np.zeros((cfg.height, cfg.width, 4), np.uint8) if image else None
+    ms = C.c_double()
+    e = _err()
+    _check(lib().fpt_cuda_voxel_render(C.byref(cfg), C.byref(ext) if ext is not None else None,
+                                       hits.ctypes.data_as(C.POINTER(FptCudaVoxelHit)), n,
+                                       rgba.ctypes.data_as(C.POINTER(C.c_uint8)) if rgba is not None else None,
+                                       rgba.size if rgba is not None else 0, C.byref(ms), e, len(e)), e)
+    return hits.reshape(cfg.height, cfg.width), rgba, ms.value

@@ -285,5 +285,26 @@ def mandelbox_path(width: int = 1920, height: int = 1080, spp: int = 16, bounces
     return _fractal_path(mandelbox_ext(), width, height, spp, bounces, seed, (0.0, 1.5, -7.0), (0.0, 0.0, 0.0), 1e-4 / 7.0)
 
 
+def voxel_mandelbox(resolution: int = 1024, width: int = 1920, height: int = 1080):
+    """Mandelbox (scale -1.5, 12 iterations, min radius 0.5, fold limit 1) voxelized over [-4, 4]^3;
+    primary + one shadow ray per pixel through the occupancy bricks."""
+    cfg = ffi.default_config()
+    cfg.width, cfg.height, cfg.samples = width, height, 1
+    cfg.sdf_id = ffi.SDF_MANDELBOX_FRACTAL
+    cfg.renderer_backend = ffi.RENDERER_VOXEL
+    cfg.voxel_resolution = resolution
+    cfg.voxel_bounds_min[:] = [-4.0, -4.0, -4.0]
+    cfg.voxel_bounds_max[:] = [4.0, 4.0, 4.0]
+    cfg.voxel_surface_band = 1.0
+    cfg.camera_fov = fov_for_vertical(50.0)
+    cfg.camera_dof = 0.0
+    cfg.focus_distance = 8.0
+    look_at(cfg, (5.5, 4.0, -9.0), (0.0, 0.0, 0.0))
+    ext = mandelbox_ext()
+    ext.sun_direction[:] = [0.3, 0.8, 0.5]
+    ext.sun_intensity = 1.0
+    return cfg, ext
+
+
 def temp_path(name: str) -> str:
     return os.path.join(tempfile.gettempdir(), name)

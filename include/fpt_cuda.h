@@ -648,6 +648,81 @@ int fpt_cuda_sample_distance(const struct FptRenderConfig *config,
                              char *error,
                              size_t error_len);
 
+/* Resident voxel grid built by fpt_cuda_voxel_build. */
+struct FptCudaVoxelInfo {
+    uint32_t resolution;
+    uint32_t brick_size;      /* 8: occupancy bricks, 4: reference cells, 0: dense reference cells */
+    uint32_t brick_grid;      /* bricks per axis */
+    uint32_t active_bricks;
+    uint64_t active_cells;
+    uint64_t memory_bytes;    /* brick table + payload */
+    double build_ms;
+};
+
+/* One traced voxel ray. */
+struct FptCudaVoxelHit {
+    float t;                  /* entry distance of the first occupied cell, -1 on a miss */
+    uint32_t cell;            /* x + y*res + z*res^2 of that cell, 0xffffffff on a miss */
+    uint32_t normal_axis;     /* face entered: 1 +x, 2 -x, 3 +y, 4 -y, 5 +z, 6 -z (0 = none) */
+    uint32_t steps;           /* cells visited by the primary ray */
+    uint32_t shadow_steps;    /* cells visited by the shadow ray */
+    uint32_t lit;             /* 1 when the shadow ray escaped (sequence call: 1 on hit) */
+};
+
+/* Voxelizes the scene's distance estimator over FptRenderConfig's voxel
+ * bounds and resolution and keeps the grid resident for the calls below
+ * (classifier shaders/Shaders.metal:4196-4244, legacy coverage;
+ * buildVoxelCell 5388-5414; brick ids in raster order as the host
+ * compaction of src/metal_bridge.mm:1738-1812).  brick_size 8 builds
+ * occupancy bricks (uint8 occupancy + fp16 distance per cell, uint32
+ * brick table, 0 = empty else index + 1); 4 builds the reference's 4^3
+ * bricks of 12-byte cells; 0 the reference's dense cells. */
+int fpt_cuda_voxel_build(const struct FptRenderConfig *config,
+                         const struct FptCudaSceneExt *ext,
+                         uint32_t brick_size,
+                         struct FptCudaVoxelInfo *info,
+                         char *error,
+                         size_t error_len);
+
+/* Copies the resident grid to the host: brick table (brick_grid^3 words),
+ * and per compact cell the occupancy bytes and fp16 distances (occupancy
+ * bricks) or the 3-word reference cells. NULL skips an output. */
+int fpt_cuda_voxel_read(uint32_t *brick_table,
+                        size_t table_len,
+                        uint8_t *occupancy,
+                        uint16_t *distance,
+                        uint32_t *cells,
+                        size_t cell_len,
+                        char *error,
+                        size_t error_len);
+
+/* Traces ray_count rays (origin xyz, direction xyz per ray) through the
+ * resident grid with the exact DDA of traceVoxel (shaders/Shaders.metal:
+ * 4492-4612) and records every visited cell (x + y*res + z*res^2), up to
+ * `capacity` per ray; sequence_len gets the full visit count. */
+int fpt_cuda_dda_sequence(const float *rays,
+                          size_t ray_count,
+                          uint32_t capacity,
+                          uint32_t *sequence,
+                          uint32_t *sequence_len,
+                          struct FptCudaVoxelHit *hits,
+                          char *error,
+                          size_t error_len);
+
+/* Primary ray per pixel centre plus one sun shadow ray per hit through the
+ * resident occupancy-brick grid (legacy origin offset, shaders/Shaders.metal:
+ * 4068-4089).  hits: width*height, row 0 at the bottom; rgba (optional):
+ * shaded image, row 0 at the top. */
+int fpt_cuda_voxel_render(const struct FptRenderConfig *config,
+                          const struct FptCudaSceneExt *ext,
+                          struct FptCudaVoxelHit *hits,
+                          size_t hit_count,
+                          uint8_t *rgba,
+                          size_t rgba_len,
+                          double *elapsed_ms,
+                          char *error,
+                          size_t error_len);
+
 #ifdef __cplusplus
 }
 #endif

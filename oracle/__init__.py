@@ -35,6 +35,16 @@ def lib() -> C.CDLL:
         L.oracle_render_path.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, P(C.c_float)]
         L.oracle_present.argtypes = [vp, P(C.c_float), P(C.c_uint8)]
         L.oracle_image_metrics.argtypes = [P(C.c_uint8), P(C.c_uint8), C.c_uint32, C.c_uint32, P(C.c_double)]
+        L.oracle_voxel_build.argtypes = [vp, vp, C.c_uint32, P(C.c_uint32), P(C.c_uint8), P(C.c_uint16), P(C.c_uint32),
+                                         C.c_size_t, P(C.c_ulonglong)]
+        L.oracle_voxel_build.restype = C.c_longlong
+        L.oracle_voxel_brick.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_uint8), P(C.c_uint16)]
+        L.oracle_dda.argtypes = [vp, C.c_uint32, P(C.c_uint32), P(C.c_uint8), P(C.c_uint32), P(C.c_float), C.c_size_t,
+                                 C.c_uint32, P(C.c_uint32), P(C.c_uint32), P(C.c_double)]
+        L.oracle_voxel_primary.argtypes = [vp, vp, P(C.c_uint32), P(C.c_uint8), C.c_uint32, C.c_uint32, P(C.c_double)]
+        L.oracle_dda_contract.restype = C.c_uint32
+        L.oracle_float_to_half.argtypes = [C.c_float]
+        L.oracle_float_to_half.restype = C.c_uint16
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_max_threads.restype = C.c_int
         _lib = L
@@ -115,3 +125,60 @@ def image_metrics(a, b):
     lib().oracle_image_metrics(a.ctypes.data_as(C.POINTER(C.c_uint8)), b.ctypes.data_as(C.POINTER(C.c_uint8)),
                                a.shape[1], a.shape[0], out.ctypes.data_as(C.POINTER(C.c_double)))
     return dict(zip(["mae", "rmse", "max_abs", "changed_pct", "ssim", "lf_ssim"], out.tolist()))
+
+
+def _p(a, ty):
+    return a.ctypes.data_as(C.POINTER(ty)) if a is not None else None
+
+
+def voxel_build(cfg, ext, brick_size=8, max_cells=None):
+    """CPU build: (table, occupancy, distance-as-fp16-bits or None, cells or None, active_cells)."""
+    res = cfg.voxel_resolution
+    bg = (res + brick_size - 1) // brick_size
+    table = np.zeros(bg ** 3, np.uint32)
+    cap = max_cells if max_cells is not None else bg ** 3 * brick_size ** 3
+    occ = np.zeros(cap, np.uint8) if brick_size == 8 else None
+    dist = np.zeros(cap, np.uint16) if brick_size == 8 else None
+    cells = np.zeros((cap, 3), np.uint32) if brick_size != 8 else None
+    active_cells = C.c_ulonglong()
+    n = lib().oracle_voxel_build(_ref(cfg), _ref(ext), brick_size, _p(table, C.c_uint32), _p(occ, C.c_uint8), _p(dist, C.c_uint16),
+                                 _p(cells, C.c_uint32), cap, C.byref(active_cells))
+    if n < 0:
+        raise ValueError("cell capacity too small")
+    m = int(n) * brick_size ** 3
+    return (table, occ[:m] if occ is not None else None, dist[:m] if dist is not None else None,
+            cells[:m] if cells is not None else None, active_cells.value)
+
+
+def voxel_brick(cfg, ext, brick_size, bx, by, bz):
+    occ = np.zeros(brick_size ** 3, np.uint8)
+    dist = np.zeros(brick_size ** 3, np.uint16)
+    lib().oracle_voxel_brick(_ref(cfg), _ref(ext), brick_size, bx, by, bz, _p(occ, C.c_uint8), _p(dist, C.c_uint16))
+    return occ, dist
+
+
+def dda(cfg, brick_size, table, occ, cells, rays, capacity=0):
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    n = len(r)
+    seq = np.zeros((n, capacity), np.uint32) if capacity else None
+    seq_len = np.zeros(n, np.uint32) if capacity else None
+    hits = np.zeros((n, 4), np.float64)
+    lib().oracle_dda(_ref(cfg), brick_size, _p(table, C.c_uint32), _p(occ, C.c_uint8),
+                     _p(np.ascontiguousarray(cells, np.uint32) if cells is not None else None, C.c_uint32),
+                     _p(r, C.c_float), n, capacity, _p(seq, C.c_uint32), _p(seq_len, C.c_uint32), _p(hits, C.c_double))
+    return hits, seq, seq_len
+
+
+def voxel_primary(cfg, ext, table, occ, rows=None):
+    y0, y1 = rows if rows is not None else (0, cfg.height)
+    out = np.zeros((cfg.height, cfg.width, 5), np.float64)
+    lib().oracle_voxel_primary(_ref(cfg), _ref(ext), _p(table, C.c_uint32), _p(occ, C.c_uint8), y0, y1, _p(out, C.c_double))
+    return out
+
+
+def dda_contract():
+    return int(lib().oracle_dda_contract())
+
+
+def float_to_half(values):
+    return np.array([lib().oracle_float_to_half(float(v)) for v in np.asarray(values, np.float32)], np.uint16)

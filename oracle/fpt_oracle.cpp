@@ -1809,3 +1809,376 @@ void oracle_image_metrics(const uint8_t *a, const uint8_t *b, uint32_t W, uint32
 }
 
 }  // extern "C"
+
+// ====================================================================== voxels
+// CPU restatement of the voxel classifier (shaders/Shaders.metal:4196-4244,
+// legacy coverage), buildVoxelCell (5388-5414), the raster-order host
+// compaction (src/metal_bridge.mm:1738-1812) and the DDA traversal
+// (4091-4190, traceVoxel 4492-4612).  Compiled without contraction, so the
+// same float operations give the same bits as the GPU build.
+namespace oracle {
+
+struct VGrid {
+    float bmin[3], bmax[3], cs[3];
+    uint32_t res, bs, bg;      // resolution, brick size, bricks per axis
+    uint32_t storage;          // 0 dense reference cells, 1 reference bricks, 4 occupancy bricks
+    const uint32_t *table;
+    const uint8_t *occ;
+    const uint32_t *cells;
+};
+
+inline bool classify(const Cfg &c, const Ext &e, const float bmin[3], const float cs[3], float radius, uint32_t x, uint32_t y,
+                     uint32_t z, float &d, V3<float> &p) {
+    p = V3<float>(bmin[0] + (float(x) + 0.5f) * cs[0], bmin[1] + (float(y) + 0.5f) * cs[1], bmin[2] + (float(z) + 0.5f) * cs[2]);
+    d = distanceSdf(p, c, e);
+    bool occ = std::isfinite(d) && std::fabs(d) <= radius * std::max(c.voxel_surface_band, 0.25f);
+    if (c.voxel_fill_interior != 0u && std::isfinite(d) && d < 0.0f) occ = true;
+    return occ;
+}
+
+// IEEE binary16 round-to-nearest-even (the conversion __float2half_rn performs).
+inline uint16_t float_to_half_rne(float f) {
+    uint32_t x = float_bits(f);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t ax = x & 0x7fffffffu;
+    if (ax >= 0x7f800000u) return uint16_t(sign | 0x7c00u | (ax > 0x7f800000u ? 0x200u : 0u));
+    if (ax >= 0x477ff000u) return uint16_t(sign | 0x7c00u);   // rounds to infinity
+    if (ax < 0x38800000u) {                                    // subnormal half or zero
+        if (ax < 0x33000000u) return uint16_t(sign);           // below half of the smallest subnormal
+        uint32_t e = ax >> 23;
+        uint32_t m = (ax & 0x7fffffu) | 0x800000u;
+        uint32_t shift = 126u - e;
+        uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1u);
+        if (rem > half || (rem == half && (q & 1u))) ++q;
+        return uint16_t(sign | q);
+    }
+    uint32_t e = (ax >> 23) - 112u;
+    uint32_t m = ax & 0x7fffffu;
+    uint32_t q = (e << 10) | (m >> 13);
+    uint32_t rem = m & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (q & 1u))) ++q;
+    return uint16_t(sign | q);
+}
+
+inline uint32_t pack_unorm4(float a, float b, float c, float d) {
+    auto q = [](float v) { return uint32_t(std::nearbyint(std::min(std::max(v, 0.0f), 1.0f) * 255.0f)); };
+    return q(a) | (q(b) << 8) | (q(c) << 16) | (q(d) << 24);
+}
+
+inline bool ray_aabb(V3<float> o, V3<float> d, const float *bmin, const float *bmax, float &near_t, float &far_t, V3<float> &en) {
+    near_t = -kInf;
+    far_t = kInf;
+    en = V3<float>(0.f);
+    for (int a = 0; a < 3; ++a) {
+        if (d[a] == 0.0f) {
+            if (o[a] < bmin[a] || o[a] > bmax[a]) return false;
+            continue;
+        }
+        float t0 = (bmin[a] - o[a]) / d[a], t1 = (bmax[a] - o[a]) / d[a];
+        float an = std::min(t0, t1), af = std::max(t0, t1);
+        if (an > near_t) {
+            near_t = an;
+            en = V3<float>(0.f);
+            en[a] = d[a] > 0.0f ? -1.0f : 1.0f;
+        }
+        far_t = std::min(far_t, af);
+        if (near_t > far_t) return false;
+    }
+    float entry = std::max(near_t, 0.0f);
+    return std::isfinite(entry) && std::isfinite(far_t) && far_t >= entry;
+}
+inline bool cell_coordinate(V3<float> p, V3<float> d, const VGrid &g, int c[3]) {
+    for (int a = 0; a < 3; ++a) if (p[a] < g.bmin[a] || p[a] > g.bmax[a]) return false;
+    for (int a = 0; a < 3; ++a) if ((d[a] < 0.0f && p[a] <= g.bmin[a]) || (d[a] > 0.0f && p[a] >= g.bmax[a])) return false;
+    for (int a = 0; a < 3; ++a) {
+        float gp = (p[a] - g.bmin[a]) / g.cs[a];
+        float fl = std::floor(gp);
+        int ci = int(fl) - ((d[a] < 0.0f && gp == fl) ? 1 : 0);
+        ci = std::min(ci, int(g.res) - 1);
+        if (ci < 0 || ci >= int(g.res)) return false;
+        c[a] = ci;
+    }
+    return true;
+}
+inline float next_positive_float(float v) {
+    if (!std::isfinite(v) || v < 0.0f) return kInf;
+    if (v == 0.0f) return bits_float(1u);
+    return bits_float(float_bits(v) + 1u);
+}
+inline bool advance(int c[3], const int st[3], float nt[3], const float dt[3], float &et, V3<float> &en) {
+    float bt = std::min(nt[0], std::min(nt[1], nt[2]));
+    if (!std::isfinite(bt)) return false;
+    bool cr[3] = {nt[0] == bt, nt[1] == bt, nt[2] == bt};
+    float ne = bt;
+    if (!(ne > et)) {
+        ne = next_positive_float(et);
+        if (!std::isfinite(ne) || !(ne > et)) return false;
+    }
+    et = ne;
+    en = V3<float>(0.f);
+    int na = cr[0] ? 0 : (cr[1] ? 1 : 2);
+    en[na] = st[na] > 0 ? -1.0f : 1.0f;
+    for (int a = 0; a < 3; ++a) if (cr[a]) { c[a] += st[a]; nt[a] = nt[a] + dt[a]; }
+    return true;
+}
+inline bool occupied(const VGrid &g, const int c[3], uint32_t &payload) {
+    uint32_t x = uint32_t(c[0]), y = uint32_t(c[1]), z = uint32_t(c[2]);
+    if (g.storage == 0u) { payload = x + y * g.res + z * g.res * g.res; return (g.cells[size_t(payload) * 3] & 0x80000000u) != 0u; }
+    uint32_t b = x / g.bs + (y / g.bs) * g.bg + (z / g.bs) * g.bg * g.bg;
+    uint32_t page = g.table[b];
+    if (page == 0u) return false;
+    payload = (page - 1u) * g.bs * g.bs * g.bs + (x % g.bs) + (y % g.bs) * g.bs + (z % g.bs) * g.bs * g.bs;
+    if (g.storage == 4u) return g.occ[payload] != 0u;
+    return (g.cells[size_t(payload) * 3] & 0x80000000u) != 0u;
+}
+struct VHit { bool hit; float t; int cell[3]; V3<float> normal; uint32_t steps; };
+inline VHit trace(const VGrid &g, V3<float> o, V3<float> d, std::vector<uint32_t> *seq) {
+    VHit h{false, kInf, {0, 0, 0}, V3<float>(0.f), 0u};
+    float near_t, far_t;
+    V3<float> en;
+    if (!ray_aabb(o, d, g.bmin, g.bmax, near_t, far_t, en)) return h;
+    float et = std::max(near_t, 0.0f);
+    V3<float> start(std::min(std::max(o.x + d.x * et, g.bmin[0]), g.bmax[0]), std::min(std::max(o.y + d.y * et, g.bmin[1]), g.bmax[1]),
+                    std::min(std::max(o.z + d.z * et, g.bmin[2]), g.bmax[2]));
+    int c[3];
+    if (!cell_coordinate(start, d, g, c)) return h;
+    int st[3] = {0, 0, 0};
+    float nt[3] = {kInf, kInf, kInf}, dt[3] = {kInf, kInf, kInf};
+    for (int a = 0; a < 3; ++a) {
+        float n = kInf, dd = kInf;
+        if (d[a] > 0.0f) {
+            st[a] = 1;
+            float boundary = g.bmin[a] + float(c[a] + 1) * g.cs[a];
+            n = (boundary - o[a]) / d[a];
+            dd = g.cs[a] / d[a];
+        } else if (d[a] < 0.0f) {
+            st[a] = -1;
+            float boundary = g.bmin[a] + float(c[a]) * g.cs[a];
+            n = (boundary - o[a]) / d[a];
+            dd = -g.cs[a] / d[a];
+        }
+        if (!std::isfinite(n) || !std::isfinite(dd)) { n = kInf; dd = kInf; }
+        nt[a] = n; dt[a] = dd;
+    }
+    const uint32_t max_steps = g.res * 3u + 3u;
+    for (uint32_t s = 0; s < max_steps && et <= far_t; ++s) {
+        if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= int(g.res) || c[1] >= int(g.res) || c[2] >= int(g.res)) break;
+        if (seq) seq->push_back(uint32_t(c[0]) + uint32_t(c[1]) * g.res + uint32_t(c[2]) * g.res * g.res);
+        uint32_t payload = 0;
+        if (occupied(g, c, payload)) {
+            h.hit = true; h.t = et; h.cell[0] = c[0]; h.cell[1] = c[1]; h.cell[2] = c[2]; h.normal = en; h.steps = s + 1;
+            return h;
+        }
+        if (!advance(c, st, nt, dt, et, en)) break;
+    }
+    return h;
+}
+
+}  // namespace oracle
+
+extern "C" {
+
+// Builds the voxel grid on the CPU.  brick_size 8: occupancy bricks (occ,
+// dist per compact cell); 4: reference cells (3 words per compact cell).
+// Returns the number of active bricks, or -1 when cell_cap is too small.
+long long oracle_voxel_build(const FptRenderConfig *cfg, const FptCudaSceneExt *e, uint32_t brick_size, uint32_t *table, uint8_t *occ,
+                             uint16_t *dist, uint32_t *cells, size_t cell_cap, unsigned long long *active_cells) {
+    const Ext &ex = ext_or_default(e);
+    const FptRenderConfig &c = *cfg;
+    uint32_t res = c.voxel_resolution, bs = brick_size, bg = (res + bs - 1) / bs;
+    float bmin[3], cs[3];
+    for (int k = 0; k < 3; ++k) { bmin[k] = c.voxel_bounds_min[k]; cs[k] = (c.voxel_bounds_max[k] - c.voxel_bounds_min[k]) / float(res); }
+    float hx = cs[0] * 0.5f, hy = cs[1] * 0.5f, hz = cs[2] * 0.5f;
+    float radius = std::sqrt(hx * hx + hy * hy + hz * hz);
+    size_t nb = size_t(bg) * bg * bg;
+    std::vector<uint32_t> count(nb, 0);
+    unsigned long long cells_total = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : cells_total)
+    for (long long b = 0; b < (long long)nb; ++b) {
+        uint32_t bx = uint32_t(b % bg), by = uint32_t((b / bg) % bg), bz = uint32_t(b / (size_t(bg) * bg));
+        uint32_t n = 0;
+        for (uint32_t l = 0; l < bs * bs * bs; ++l) {
+            uint32_t x = bx * bs + l % bs, y = by * bs + (l / bs) % bs, z = bz * bs + l / (bs * bs);
+            if (x >= res || y >= res || z >= res) continue;
+            float d; V3<float> p;
+            if (classify(c, ex, bmin, cs, radius, x, y, z, d, p)) ++n;
+        }
+        count[size_t(b)] = n;
+        cells_total += n;
+    }
+    uint32_t active = 0;
+    for (size_t b = 0; b < nb; ++b) table[b] = count[b] ? ++active : 0u;   // raster order, x fastest
+    if (active_cells) *active_cells = cells_total;
+    size_t bvol = size_t(bs) * bs * bs;
+    if (size_t(active) * bvol > cell_cap) return -1;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long long b = 0; b < (long long)nb; ++b) {
+        if (!table[b]) continue;
+        uint32_t bx = uint32_t(b % bg), by = uint32_t((b / bg) % bg), bz = uint32_t(b / (size_t(bg) * bg));
+        size_t base = size_t(table[b] - 1) * bvol;
+        for (uint32_t l = 0; l < bs * bs * bs; ++l) {
+            uint32_t x = bx * bs + l % bs, y = by * bs + (l / bs) % bs, z = bz * bs + l / (bs * bs);
+            bool inside = x < res && y < res && z < res;
+            float d = 0.0f; V3<float> p;
+            bool o = inside && classify(c, ex, bmin, cs, radius, x, y, z, d, p);
+            if (occ) occ[base + l] = o ? 1u : 0u;
+            if (dist) dist[base + l] = float_to_half_rne(inside ? d : 0.0f);
+            if (cells) {
+                uint32_t c0 = 0, c1 = 0, c2 = 0;
+                if (o) {
+                    Material<float> m = userMaterial(p, c, ex);
+                    c0 = pack_unorm4(m.rgb.x, m.rgb.y, m.rgb.z, 0.0f) | 0x80000000u;
+                    c1 = pack_unorm4(m.roughness, m.specular, m.translucency, (m.ior - 1.0f) / 1.5f);
+                    c2 = float_bits(m.emission);
+                }
+                cells[(base + l) * 3] = c0; cells[(base + l) * 3 + 1] = c1; cells[(base + l) * 3 + 2] = c2;
+            }
+        }
+    }
+    return (long long)active;
+}
+
+// Occupancy and fp16 distance of the cells of one brick (spot checks at full size).
+void oracle_voxel_brick(const FptRenderConfig *cfg, const FptCudaSceneExt *e, uint32_t brick_size, uint32_t bx, uint32_t by,
+                        uint32_t bz, uint8_t *occ, uint16_t *dist) {
+    const Ext &ex = ext_or_default(e);
+    const FptRenderConfig &c = *cfg;
+    uint32_t res = c.voxel_resolution, bs = brick_size;
+    float bmin[3], cs[3];
+    for (int k = 0; k < 3; ++k) { bmin[k] = c.voxel_bounds_min[k]; cs[k] = (c.voxel_bounds_max[k] - c.voxel_bounds_min[k]) / float(res); }
+    float hx = cs[0] * 0.5f, hy = cs[1] * 0.5f, hz = cs[2] * 0.5f;
+    float radius = std::sqrt(hx * hx + hy * hy + hz * hz);
+    for (uint32_t l = 0; l < bs * bs * bs; ++l) {
+        uint32_t x = bx * bs + l % bs, y = by * bs + (l / bs) % bs, z = bz * bs + l / (bs * bs);
+        bool inside = x < res && y < res && z < res;
+        float d = 0.0f; V3<float> p;
+        bool o = inside && classify(c, ex, bmin, cs, radius, x, y, z, d, p);
+        occ[l] = o ? 1u : 0u;
+        dist[l] = float_to_half_rne(inside ? d : 0.0f);
+    }
+}
+
+// Traces rays (6 floats each) through a grid given as arrays; records up to
+// cap cells per ray.  out_hits: n x {t, cell, steps, hit} as doubles.
+void oracle_dda(const FptRenderConfig *cfg, uint32_t brick_size, const uint32_t *table, const uint8_t *occ, const uint32_t *cells,
+                const float *rays, size_t n, uint32_t cap, uint32_t *seq, uint32_t *seq_len, double *out_hits) {
+    VGrid g;
+    const FptRenderConfig &c = *cfg;
+    for (int k = 0; k < 3; ++k) {
+        g.bmin[k] = c.voxel_bounds_min[k]; g.bmax[k] = c.voxel_bounds_max[k];
+        g.cs[k] = (c.voxel_bounds_max[k] - c.voxel_bounds_min[k]) / float(c.voxel_resolution);
+    }
+    g.res = c.voxel_resolution; g.bs = brick_size ? brick_size : 1; g.bg = brick_size ? (g.res + brick_size - 1) / brick_size : 0;
+    g.storage = brick_size == 8 ? 4u : (brick_size == 0 ? 0u : 1u);
+    g.table = table; g.occ = occ; g.cells = cells;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long i = 0; i < (long long)n; ++i) {
+        const float *r = rays + i * 6;
+        std::vector<uint32_t> s;
+        VHit h = trace(g, V3<float>(r[0], r[1], r[2]), V3<float>(r[3], r[4], r[5]), seq ? &s : nullptr);
+        if (seq) {
+            seq_len[i] = uint32_t(s.size());
+            for (size_t k = 0; k < s.size() && k < cap; ++k) seq[size_t(i) * cap + k] = s[k];
+        }
+        double *o = out_hits + i * 4;
+        o[0] = h.hit ? double(h.t) : -1.0;
+        o[1] = h.hit ? double(uint32_t(h.cell[0]) + uint32_t(h.cell[1]) * g.res + uint32_t(h.cell[2]) * g.res * g.res) : -1.0;
+        o[2] = h.steps;
+        o[3] = h.hit ? 1.0 : 0.0;
+    }
+}
+
+// Primary + shadow ray per pixel centre through an occupancy-brick grid
+// (pixel rows [y0, y1)); out: W*H x {t, cell, lit, steps, shadow_steps}.
+void oracle_voxel_primary(const FptRenderConfig *cfg, const FptCudaSceneExt *e, const uint32_t *table, const uint8_t *occ, uint32_t y0,
+                          uint32_t y1, double *out) {
+    const FptRenderConfig &c = *cfg;
+    VGrid g;
+    for (int k = 0; k < 3; ++k) {
+        g.bmin[k] = c.voxel_bounds_min[k]; g.bmax[k] = c.voxel_bounds_max[k];
+        g.cs[k] = (c.voxel_bounds_max[k] - c.voxel_bounds_min[k]) / float(c.voxel_resolution);
+    }
+    g.res = c.voxel_resolution; g.bs = 8; g.bg = (g.res + 7) / 8; g.storage = 4; g.table = table; g.occ = occ; g.cells = nullptr;
+    float sun[3];
+    if (e && e->sun_intensity > 0.0f) {
+        float n = std::sqrt(e->sun_direction[0] * e->sun_direction[0] + e->sun_direction[1] * e->sun_direction[1] +
+                            e->sun_direction[2] * e->sun_direction[2]);
+        for (int k = 0; k < 3; ++k) sun[k] = e->sun_direction[k] / n;
+    } else {
+        float yaw = c.sun[1] * 3.14159265359f / 180.0f, pitch = c.sun[2] * 3.14159265359f / 180.0f;
+        float y = std::sin(pitch), z = std::cos(pitch);
+        sun[0] = z * std::sin(yaw); sun[1] = y; sun[2] = z * std::cos(yaw);
+    }
+    float focal = 1.0f / std::tan(c.camera_fov / 2.0f * 3.14159265359f / 180.0f);
+    float sr = std::sin(c.camera_roll), cr = std::cos(c.camera_roll);
+    float sp = std::sin(c.camera_yaw_pitch[1]), cp = std::cos(c.camera_yaw_pitch[1]);
+    float sy = std::sin(c.camera_yaw_pitch[0]), cy = std::cos(c.camera_yaw_pitch[0]);
+    float eps = std::min(g.cs[0], std::min(g.cs[1], g.cs[2])) * 0.01f;
+    const uint32_t W = c.width, H = c.height;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long yy = y0; yy < (long long)y1; ++yy) {
+        for (uint32_t x = 0; x < W; ++x) {
+            uint32_t y = uint32_t(yy);
+            float u = (float(x) + 0.5f) / float(W) - 0.5f, v = (float(y) + 0.5f) / float(H) - 0.5f;
+            u = u * (float(W) / float(H));
+            float len = std::sqrt(u * u + v * v + focal * focal);
+            float dx = u / len, dy = v / len, dz = focal / len;
+            float rx = cr * dx - sr * dy, ry = sr * dx + cr * dy;
+            dx = rx; dy = ry;
+            float y1b = dz * sp + dy * cp, z1b = dz * cp - dy * sp;
+            dy = y1b; dz = z1b;
+            V3<float> d(dx * cy + dz * sy, dy, -dx * sy + dz * cy);
+            V3<float> o(c.camera_position[0], c.camera_position[1], c.camera_position[2]);
+            VHit h = trace(g, o, d, nullptr);
+            double *r = out + (size_t(y) * W + x) * 5;
+            r[0] = h.hit ? double(h.t) : -1.0;
+            r[1] = h.hit ? double(uint32_t(h.cell[0]) + uint32_t(h.cell[1]) * g.res + uint32_t(h.cell[2]) * g.res * g.res) : -1.0;
+            r[2] = 0.0; r[3] = h.steps; r[4] = 0.0;
+            if (h.hit) {
+                V3<float> pos(o.x + d.x * h.t, o.y + d.y * h.t, o.z + d.z * h.t);
+                V3<float> n = h.normal;
+                if (n.x * d.x + n.y * d.y + n.z * d.z > 0.0f) n = V3<float>(-n.x, -n.y, -n.z);
+                float side = (sun[0] * n.x + sun[1] * n.y + sun[2] * n.z) >= 0.0f ? 1.0f : -1.0f;
+                V3<float> so(pos.x + n.x * side * eps, pos.y + n.y * side * eps, pos.z + n.z * side * eps);
+                VHit s = trace(g, so, V3<float>(sun[0], sun[1], sun[2]), nullptr);
+                r[2] = s.hit ? 0.0 : 1.0;
+                r[4] = s.steps;
+            }
+        }
+    }
+}
+
+// voxel_dda_contract_test cases (shaders/Shaders.metal:5164-5211); bit k = failed case k.
+uint32_t oracle_dda_contract(void) {
+    uint32_t f = 0u;
+    VGrid g;
+    for (int k = 0; k < 3; ++k) { g.bmin[k] = 0.0f; g.bmax[k] = 4.0f; g.cs[k] = 1.0f; }
+    g.res = 4; g.bs = 4; g.bg = 1; g.storage = 1; g.table = nullptr; g.occ = nullptr; g.cells = nullptr;
+    int c[3];
+    auto eq = [&](int x, int y, int z) { return c[0] == x && c[1] == y && c[2] == z; };
+    if (!cell_coordinate(V3<float>(1, 2, 3), V3<float>(1, 1, 1), g, c) || !eq(1, 2, 3)) f |= 1u << 0;
+    if (!cell_coordinate(V3<float>(1, 2, 3), V3<float>(-1, -1, -1), g, c) || !eq(0, 1, 2)) f |= 1u << 1;
+    if (!cell_coordinate(V3<float>(4, 4, 4), V3<float>(-1, -1, -1), g, c) || !eq(3, 3, 3)) f |= 1u << 2;
+    if (cell_coordinate(V3<float>(4, 4, 4), V3<float>(1, 1, 1), g, c)) f |= 1u << 3;
+    if (!cell_coordinate(V3<float>(4, 4, 4), V3<float>(0, 0, 0), g, c) || !eq(3, 3, 3)) f |= 1u << 4;
+    c[0] = c[1] = c[2] = 0;
+    int st[3] = {1, 1, 1};
+    float nt[3] = {1, 1, 2}, dt[3] = {1, 1, 1}, et = 0.0f;
+    V3<float> en;
+    if (!advance(c, st, nt, dt, et, en) || !eq(1, 1, 0) || nt[0] != 2 || nt[1] != 2 || nt[2] != 2 || et != 1.0f || en.x != -1.0f ||
+        en.y != 0.0f || en.z != 0.0f)
+        f |= 1u << 5;
+    if (!advance(c, st, nt, dt, et, en) || !eq(2, 2, 1) || nt[0] != 3 || nt[1] != 3 || nt[2] != 3 || et != 2.0f) f |= 1u << 6;
+    c[0] = c[1] = c[2] = 0;
+    nt[0] = 1; nt[1] = 2; nt[2] = 3;
+    et = 1.0f;
+    if (!advance(c, st, nt, dt, et, en) || float_bits(et) != float_bits(1.0f) + 1u || !eq(1, 0, 0)) f |= 1u << 7;
+    float nr, fr;
+    if (!ray_aabb(V3<float>(-1, 2, 2), V3<float>(1.0e-9f, 0, 0), g.bmin, g.bmax, nr, fr, en) || !(nr > 0.0f) || !(fr > nr)) f |= 1u << 8;
+    if (ray_aabb(V3<float>(-1, 5, 2), V3<float>(1, 0, 0), g.bmin, g.bmax, nr, fr, en)) f |= 1u << 9;
+    return f;
+}
+
+uint16_t oracle_float_to_half(float f) { return float_to_half_rne(f); }
+
+}  // extern "C"
