@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -837,3 +838,160 @@ int fpt_cuda_voxel_render(const struct FptRenderConfig *config, const struct Fpt
 }
 
 }  // extern "C"
+
+// ====================================================================== build without allocation
+// fpt_cuda_voxel_build_static: the occupancy-brick build for callers that
+// cannot allocate device memory.  Its scratch (scene block, per-brick
+// counts and offsets, scan partials, counters) is one file-scope device
+// array of fixed size, so the entry point calls no cudaMalloc, cudaFree or
+// allocating library routine; the caller passes the outputs.
+namespace fpt {
+
+constexpr uint32_t kStaticMaxResolution = 512;                    // 8^3 bricks: at most 64^3 of them
+constexpr uint32_t kStaticMaxBricks = 64u * 64u * 64u;
+constexpr uint32_t kStaticScanBlocks = (kStaticMaxBricks + kScanBlock - 1) / kScanBlock;
+
+struct StaticVoxelScratch {
+    unsigned long long stats[8];            // [0] active cells, [1] low word: active bricks
+    uint32_t sums[kStaticScanBlocks + 32];
+    uint32_t count[kStaticMaxBricks];
+    uint32_t offset[kStaticMaxBricks];
+    DeviceScene scene;
+};
+
+// About 2.1 MB, held by every GPU that loads the library until the process exits.
+static __device__ __align__(256) StaticVoxelScratch g_voxel_static_scratch;
+
+// Device address of g_voxel_static_scratch per device ordinal (the host-side
+// name is only a stand-in and must never be passed to a kernel).
+constexpr int kStaticMaxDevices = 64;
+static StaticVoxelScratch *g_static_scratch_addr[kStaticMaxDevices] = {nullptr};
+
+template <int KIND>
+__global__ void __launch_bounds__(512) static_fill_kernel(const DeviceScene *scene, VoxBuild B, const uint32_t *brick_count,
+                                                          const uint32_t *brick_offset, uint32_t *table, uint8_t *occ_out,
+                                                          uint16_t *dist_out, size_t cell_capacity) {
+    const DeviceScene &S = *scene;
+    uint32_t b = blockIdx.x;
+    if (brick_count[b] == 0u) {
+        if (threadIdx.x == 0) table[b] = 0u;
+        return;
+    }
+    uint32_t id = brick_offset[b];
+    if (threadIdx.x == 0) table[b] = id + 1u;
+    uint32_t bx = b % B.brick_grid, by = (b / B.brick_grid) % B.brick_grid, bz = b / (B.brick_grid * B.brick_grid);
+    uint32_t l = threadIdx.x;
+    uint32_t x = bx * 8u + l % 8u, y = by * 8u + (l / 8u) % 8u, z = bz * 8u + l / 64u;
+    bool inside = x < B.res && y < B.res && z < B.res;
+    bool occ = false;
+    float d = 0.0f;
+    float3 p;
+    if (inside) occ = classify_cell<KIND>(S, B, x, y, z, d, p);
+    size_t slot = size_t(id) * 512u + l;
+    if (slot < cell_capacity) {
+        occ_out[slot] = occ ? 1u : 0u;
+        dist_out[slot] = __half_as_ushort(__float2half_rn(inside ? d : 0.0f));
+    }
+}
+
+}  // namespace fpt
+
+extern "C" int fpt_cuda_voxel_build_static(const struct FptRenderConfig *config, const struct FptCudaSceneExt *ext, void *stream,
+                                           uint32_t *device_brick_table, size_t table_len, uint8_t *device_occupancy,
+                                           uint16_t *device_distance, size_t cell_capacity, struct FptCudaVoxelInfo *info,
+                                           char *error, size_t error_len) {
+    using namespace fpt;
+    if (info) std::memset(info, 0, sizeof(*info));
+    if (!config || !device_brick_table || !device_occupancy || !device_distance) {
+        set_error(error, error_len, "missing voxel build input or output buffer");
+        return 1;
+    }
+    const uint32_t res = config->voxel_resolution;
+    if (res == 0 || res > kStaticMaxResolution) {
+        set_error(error, error_len, "voxel resolution %u out of range for the allocation-free build (1..%u)", res,
+                  kStaticMaxResolution);
+        return 1;
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (!(config->voxel_bounds_max[k] > config->voxel_bounds_min[k])) {
+            set_error(error, error_len, "voxel bounds must be increasing on every axis");
+            return 1;
+        }
+    }
+    const uint32_t bg = (res + 7u) / 8u;
+    const uint32_t nb = bg * bg * bg;
+    if (table_len < nb) {
+        set_error(error, error_len, "brick table buffer too small (%zu < %u)", table_len, nb);
+        return 1;
+    }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    DeviceScene S;
+    if (!compile_scene(*config, ext, S, error, error_len)) return 1;
+    if (S.sky_width || S.surrogate) {
+        set_error(error, error_len, "sky textures and surrogate models are not used by the voxel build; clear them");
+        return 1;
+    }
+    int dev = 0;
+    if (!check(cudaGetDevice(&dev), "cudaGetDevice", error, error_len)) return 1;
+    if (dev < 0 || dev >= kStaticMaxDevices) { set_error(error, error_len, "device ordinal %d out of range", dev); return 1; }
+    // Set-up, once per device, with that device current: the device address of the scratch array.
+    if (!g_static_scratch_addr[dev]) {
+        void *addr = nullptr;
+        if (!check(cudaGetSymbolAddress(&addr, g_voxel_static_scratch), "cudaGetSymbolAddress", error, error_len)) return 1;
+        g_static_scratch_addr[dev] = static_cast<StaticVoxelScratch *>(addr);
+    }
+    StaticVoxelScratch *sc = g_static_scratch_addr[dev];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    VoxBuild B;
+    for (int k = 0; k < 3; ++k) {
+        B.bmin[k] = config->voxel_bounds_min[k];
+        B.cs[k] = (config->voxel_bounds_max[k] - config->voxel_bounds_min[k]) / float(res);
+    }
+    float hx = B.cs[0] * 0.5f, hy = B.cs[1] * 0.5f, hz = B.cs[2] * 0.5f;
+    B.half_radius = sqrtf(hx * hx + hy * hy + hz * hz);
+    B.band = config->voxel_surface_band;
+    B.res = res;
+    B.brick_grid = bg;
+    B.fill_interior = config->voxel_fill_interior;
+    auto t0 = std::chrono::steady_clock::now();
+    // The array keeps the previous call's contents: reset the counters.
+    if (!check(cudaMemcpyAsync(&sc->scene, &S, sizeof(DeviceScene), cudaMemcpyHostToDevice, st), "scene upload", error, error_len) ||
+        !check(cudaMemsetAsync(sc->stats, 0, sizeof(sc->stats), st), "counter reset", error, error_len))
+        return 1;
+    if (S.kind == KIND_BOX) brick_classify_kernel<KIND_BOX, 8><<<nb, 512, 0, st>>>(&sc->scene, B, sc->count, sc->stats);
+    else brick_classify_kernel<KIND_GENERIC, 8><<<nb, 512, 0, st>>>(&sc->scene, B, sc->count, sc->stats);
+    const uint32_t nblocks = (nb + kScanBlock - 1) / kScanBlock;
+    scan_blocks_kernel<<<nblocks, kScanThreads, 0, st>>>(sc->count, nb, sc->offset, sc->sums);
+    scan_sums_kernel<<<1, kScanThreads, 0, st>>>(sc->sums, nblocks, reinterpret_cast<uint32_t *>(sc->stats + 1));
+    scan_add_kernel<<<(nb + 255) / 256, 256, 0, st>>>(sc->offset, nb, sc->sums);
+    if (!check(cudaGetLastError(), "classification launch", error, error_len)) return 1;
+    unsigned long long counts[2] = {0, 0};
+    if (!check(cudaMemcpyAsync(counts, sc->stats, sizeof(counts), cudaMemcpyDeviceToHost, st), "count readback", error, error_len) ||
+        !check(cudaStreamSynchronize(st), "voxel classification", error, error_len))
+        return 1;
+    const uint32_t active = uint32_t(counts[1] & 0xffffffffull);
+    const size_t need = size_t(active) * 512u;
+    if (need > cell_capacity) {
+        set_error(error, error_len, "cell buffers too small: %u active bricks need %zu cells (capacity %zu)", active, need,
+                  cell_capacity);
+        return 1;
+    }
+    if (S.kind == KIND_BOX)
+        static_fill_kernel<KIND_BOX><<<nb, 512, 0, st>>>(&sc->scene, B, sc->count, sc->offset, device_brick_table, device_occupancy,
+                                                         device_distance, cell_capacity);
+    else
+        static_fill_kernel<KIND_GENERIC><<<nb, 512, 0, st>>>(&sc->scene, B, sc->count, sc->offset, device_brick_table,
+                                                             device_occupancy, device_distance, cell_capacity);
+    if (!check(cudaGetLastError(), "fill launch", error, error_len) || !check(cudaStreamSynchronize(st), "voxel fill", error, error_len))
+        return 1;
+    if (info) {
+        info->resolution = res;
+        info->brick_size = 8;
+        info->brick_grid = bg;
+        info->active_bricks = active;
+        info->active_cells = counts[0];
+        info->memory_bytes = size_t(nb) * 4 + need * 3;
+        info->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return 0;
+}

@@ -33,7 +33,10 @@ def declare(L: C.CDLL) -> None:
                                         P(FptCudaVoxelHit)] + err
     L.fpt_cuda_voxel_render.argtypes = [cfg, ext, P(FptCudaVoxelHit), C.c_size_t, P(C.c_uint8), C.c_size_t,
                                         P(C.c_double)] + err
-    for name in ("fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render"):
+    L.fpt_cuda_voxel_build_static.argtypes = [cfg, ext, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+                                              C.c_size_t, P(FptCudaVoxelInfo)] + err
+    for name in ("fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render",
+                 "fpt_cuda_voxel_build_static"):
         getattr(L, name).restype = C.c_int
 
 
@@ -98,3 +101,15 @@ def voxel_render(cfg, ext=None, image=True):
                                        rgba.ctypes.data_as(C.POINTER(C.c_uint8)) if rgba is not None else None,
                                        rgba.size if rgba is not None else 0, C.byref(ms), e, len(e)), e)
     return hits.reshape(cfg.height, cfg.width), rgba, ms.value
+
+
+def voxel_build_static(cfg, ext, device_table: int, table_len: int, device_occupancy: int, device_distance: int,
+                       cell_capacity: int, stream: int | None = None) -> dict:
+    """fpt_cuda_voxel_build_static: builds into caller-owned device buffers without allocating."""
+    from .native import lib
+    info = FptCudaVoxelInfo()
+    e = _err()
+    _check(lib().fpt_cuda_voxel_build_static(C.byref(cfg), C.byref(ext) if ext is not None else None, stream, device_table,
+                                             table_len, device_occupancy, device_distance, cell_capacity, C.byref(info),
+                                             e, len(e)), e)
+    return {k: getattr(info, k) for k, _ in FptCudaVoxelInfo._fields_}

@@ -723,6 +723,30 @@ int fpt_cuda_voxel_render(const struct FptRenderConfig *config,
                           char *error,
                           size_t error_len);
 
+/* Occupancy-brick voxel build that allocates nothing.  No counterpart in
+ * the reference: it serves callers that cannot allocate device memory --
+ * an engine that owns all GPU memory through its own pool, or a frame loop
+ * that cannot afford the implicit device synchronisation of cudaMalloc and
+ * cudaFree.  The caller passes device buffers for the outputs (brick table,
+ * occupancy bytes, fp16 distance bits) and a stream (NULL: the legacy
+ * default stream); the results equal fpt_cuda_voxel_build with
+ * brick_size 8.  Scratch lives in one fixed device array of about 2.1 MB
+ * that every GPU loading the library holds until the process exits, so the
+ * resolution is limited to 512.  The first call on a device looks up that
+ * array's device address; make it before any stream capture.  Every call
+ * shares the array: calls that overlap on the GPU race. */
+int fpt_cuda_voxel_build_static(const struct FptRenderConfig *config,
+                                const struct FptCudaSceneExt *ext,
+                                void *stream,
+                                uint32_t *device_brick_table,
+                                size_t table_len,
+                                uint8_t *device_occupancy,
+                                uint16_t *device_distance,
+                                size_t cell_capacity,
+                                struct FptCudaVoxelInfo *info,
+                                char *error,
+                                size_t error_len);
+
 #ifdef __cplusplus
 }
 #endif
