@@ -22,6 +22,7 @@
 #include "fpt_scene.h"
 #include "image_io.h"
 #include "bridge_internal.h"
+#include "skip.cuh"
 
 namespace fpt {
 
@@ -365,6 +366,15 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         pl.wave_scratch = c.wave;
     }
     pl.sample_rgb = c.sample_rgb;
+    SkipArgs skip;
+    if (S.surrogate) {
+        if (!ensure_buffer((void **)&c.skip_stats, &c.cap_skip_stats, kSkipStats * sizeof(unsigned long long), error, error_len) ||
+            !check(cudaMemsetAsync(c.skip_stats, 0, kSkipStats * sizeof(unsigned long long), c.stream), "skip stats reset", error,
+                   error_len) ||
+            !surrogate_args(ext->surrogate_model, S, c.skip_stats, skip, error, error_len))
+            return 1;
+        pl.skip = &skip;
+    }
     for (uint32_t start = 0; start < spp; start += step) {
         uint32_t end = std::min(spp, start + step);
         for (uint32_t a = start; a < end; a += sub_cap) {
@@ -388,6 +398,10 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
                    error_len))
             return 1;
     }
+    if (S.surrogate &&
+        !check(cudaMemcpy(c.last_skip, c.skip_stats, sizeof(c.last_skip), cudaMemcpyDeviceToHost), "skip stats readback", error,
+               error_len))
+        return 1;
     if (want_profile && profile_out) {
         unsigned long long v[8];
         if (!check(cudaMemcpy(v, c.profile, sizeof(v), cudaMemcpyDeviceToHost), "profile readback", error, error_len)) return 1;
@@ -468,11 +482,24 @@ int fpt_cuda_trace_primary(const struct FptRenderConfig *config, const struct Fp
     if (!compile_scene(hydrated, ext, S, error, error_len)) return 1;
     if (!upload_scene(S, ext, error, error_len)) return 1;
     if (!ensure_buffer((void **)&c.hits, &c.cap_hits, pixels * sizeof(FptCudaPrimaryHit), error, error_len)) return 1;
+    SkipArgs skip;
+    if (S.surrogate) {
+        if (!ensure_buffer((void **)&c.skip_stats, &c.cap_skip_stats, kSkipStats * sizeof(unsigned long long), error, error_len) ||
+            !check(cudaMemsetAsync(c.skip_stats, 0, kSkipStats * sizeof(unsigned long long), c.stream), "skip stats reset", error,
+                   error_len) ||
+            !surrogate_args(ext->surrogate_model, S, c.skip_stats, skip, error, error_len))
+            return 1;
+    }
     cudaEventRecord(c.ev0, c.stream);
-    if (!check(launch_trace_primary(S.kind, c.scene, S.width, S.height, c.hits, c.stream), "primary-ray launch", error, error_len))
-        return 1;
+    cudaError_t le = S.surrogate ? launch_skip_primary(S.kind, c.scene, S.width, S.height, skip, c.hits, c.stream)
+                                 : launch_trace_primary(S.kind, c.scene, S.width, S.height, c.hits, c.stream);
+    if (!check(le, "primary-ray launch", error, error_len)) return 1;
     cudaEventRecord(c.ev1, c.stream);
     if (!check(cudaStreamSynchronize(c.stream), "primary-ray trace", error, error_len)) return 1;
+    if (S.surrogate &&
+        !check(cudaMemcpy(c.last_skip, c.skip_stats, sizeof(c.last_skip), cudaMemcpyDeviceToHost), "skip stats readback", error,
+               error_len))
+        return 1;
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     if (elapsed_ms) *elapsed_ms = ms;

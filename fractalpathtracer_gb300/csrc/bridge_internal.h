@@ -28,6 +28,8 @@ struct Context {
     float4 *points = nullptr; size_t cap_points = 0;
     float4 *samples = nullptr; size_t cap_samples = 0;
     float *grads = nullptr; size_t cap_grads = 0;
+    unsigned long long *skip_stats = nullptr; size_t cap_skip_stats = 0;
+    unsigned long long last_skip[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // counters of the last skip-march call
     // launch tuning (set by the autotuner entry point; 0 = defaults)
     uint32_t wave_paths = 0;   // paths per wave; 0 = min(all paths, 16M)
     int march_blocks = 0;
@@ -49,6 +51,8 @@ int voxel_render_core(const FptRenderConfig &config, const FptCudaSceneExt *ext,
                       uint32_t *voxel_active_bricks, uint64_t *voxel_active_cells, double *build_ms, char *error,
                       size_t error_len);
 // mlp.cu
+struct SkipArgs;
 bool surrogate_bind(uint64_t model, DeviceScene &S, char *error, size_t error_len);
+bool surrogate_args(uint64_t model, const DeviceScene &S, unsigned long long *stats, SkipArgs &A, char *error, size_t error_len);
 
 }  // namespace fpt

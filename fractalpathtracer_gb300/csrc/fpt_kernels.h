@@ -7,6 +7,8 @@
 
 namespace fpt {
 
+struct SkipArgs;   // skip.cuh
+
 // Bytes of wave scratch per path: path record (96), two march queues (8),
 // two shadow queues (128), shade queue (4).
 constexpr size_t kWaveBytesPerPath = 96 + 8 + 128 + 4;
@@ -24,6 +26,7 @@ struct PathLaunch {
     uint32_t sample_begin, sample_end;
     int march_blocks;           // persistent march grid, <= 0 = one wave of resident blocks
     unsigned long long *profile;  // 8 device counters or null
+    const SkipArgs *skip;       // surrogate-skip pass before each march pass, or null
 };
 
 cudaError_t launch_pathtrace(const PathLaunch &pl, cudaStream_t stream);
@@ -33,6 +36,10 @@ cudaError_t launch_focus(uint32_t kind, DeviceScene *scene, cudaStream_t stream)
 cudaError_t launch_field_sample(const DeviceScene *scene, const float4 *pts, float4 *out, size_t n, cudaStream_t stream);
 cudaError_t launch_sample_distance(uint32_t kind, const DeviceScene *scene, const float4 *pts, float4 *out, float *grads, size_t n,
                                    cudaStream_t stream);
+// Labels xyz points with the scene's mapSdf distance (written to w).
+cudaError_t launch_label(uint32_t kind, const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t stream);
+cudaError_t launch_skip_primary(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, const SkipArgs &args,
+                                FptCudaPrimaryHit *hits, cudaStream_t stream);
 cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out,
                            cudaStream_t stream);
 

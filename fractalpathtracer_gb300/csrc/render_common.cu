@@ -87,7 +87,10 @@ cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, con
     cudaError_t launch_pathtrace_k##n(const PathLaunch &, cudaStream_t);                                                    \
     cudaError_t launch_trace_primary_k##n(const DeviceScene *, uint32_t, uint32_t, FptCudaPrimaryHit *, cudaStream_t);        \
     cudaError_t launch_focus_k##n(DeviceScene *, cudaStream_t);                                                              \
-    cudaError_t launch_sample_distance_k##n(const DeviceScene *, const float4 *, float4 *, float *, size_t, cudaStream_t);
+    cudaError_t launch_sample_distance_k##n(const DeviceScene *, const float4 *, float4 *, float *, size_t, cudaStream_t);       \
+    cudaError_t launch_label_k##n(const DeviceScene *, float4 *, size_t, cudaStream_t);                                      \
+    cudaError_t launch_skip_primary_k##n(const DeviceScene *, uint32_t, uint32_t, const SkipArgs &, FptCudaPrimaryHit *,     \
+                                         cudaStream_t);
 FPT_DECLARE_KIND(0)
 FPT_DECLARE_KIND(1)
 FPT_DECLARE_KIND(2)
@@ -114,6 +117,13 @@ cudaError_t launch_focus(uint32_t kind, DeviceScene *scene, cudaStream_t st) { F
 cudaError_t launch_sample_distance(uint32_t kind, const DeviceScene *scene, const float4 *pts, float4 *out, float *grads, size_t n,
                                    cudaStream_t st) {
     FPT_DISPATCH(kind, launch_sample_distance_k, scene, pts, out, grads, n, st)
+}
+cudaError_t launch_label(uint32_t kind, const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t st) {
+    FPT_DISPATCH(kind, launch_label_k, scene, pts, n, st)
+}
+cudaError_t launch_skip_primary(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, const SkipArgs &args,
+                                FptCudaPrimaryHit *hits, cudaStream_t st) {
+    FPT_DISPATCH(kind, launch_skip_primary_k, scene, W, H, args, hits, st)
 }
 
 }  // namespace fpt

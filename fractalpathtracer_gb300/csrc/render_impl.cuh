@@ -7,6 +7,7 @@
 
 #include "fpt_march.cuh"
 #include "fpt_kernels.h"
+#include "skip.cuh"
 #include "wavefront.cuh"
 
 namespace fpt {
@@ -78,6 +79,15 @@ __global__ void field_sample_kernel(const DeviceScene *scene, const float4 *poin
     float4 p = points[i];
     Field4 f = mandel_field<KIND>(mk3(p.x, p.y, p.z), *scene, 1);
     samples[i] = make_float4(f.d, f.r, f.dr, fabsf(f.state));
+}
+
+// mapSdf labels for the surrogate's training points (w <- distance).
+template <int KIND>
+__global__ void __launch_bounds__(256) label_kernel(const DeviceScene *scene, float4 *pts, size_t n) {
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pts[i];
+    pts[i].w = scene_eval<KIND>(*scene, mk3(p.x, p.y, p.z), EV_MAP).d;
 }
 
 // distanceSdf (plus orbit, derivative, iterations where defined) and the

@@ -42,6 +42,17 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<KIND>, 128, 0);
         march_blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
+    int skip_blocks = 0;
+    if (pl.skip) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(skip_march_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(skip_smem_bytes()));
+            attr = true;
+        }
+        int skip_per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&skip_per_sm, skip_march_kernel<KIND>, 32 * kSkipWarps, skip_smem_bytes());
+        skip_blocks = sms * (skip_per_sm > 0 ? skip_per_sm : 1);
+    }
     int shade_per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_per_sm, shade_kernel<KIND>, 128, 0);
     const int shade_blocks = sms * (shade_per_sm > 0 ? shade_per_sm : 1);
@@ -55,6 +66,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         for (uint32_t b = 0; b <= pl.bounces; ++b) {
             const int cur = int(b & 1u);
             reset_counters_kernel<<<1, 32, 0, stream>>>(W.counters, cur ^ 1);
+            if (pl.skip) skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, cur, *pl.skip);
             march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
             if (b < pl.bounces) shade_kernel<KIND><<<shade_blocks, 128, 0, stream>>>(W, cur);
         }
@@ -87,6 +99,22 @@ cudaError_t FPT_CAT(launch_sample_distance_k, FPT_KIND)(const DeviceScene *scene
                                                         size_t n, cudaStream_t st) {
     unsigned blocks = unsigned((n + 255) / 256);
     sample_distance_kernel<FPT_KIND><<<blocks, 256, 0, st>>>(scene, pts, out, grads, n);
+    return cudaGetLastError();
+}
+cudaError_t FPT_CAT(launch_label_k, FPT_KIND)(const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t st) {
+    label_kernel<FPT_KIND><<<unsigned((n + 255) / 256), 256, 0, st>>>(scene, pts, n);
+    return cudaGetLastError();
+}
+cudaError_t FPT_CAT(launch_skip_primary_k, FPT_KIND)(const DeviceScene *scene, uint32_t W, uint32_t H, const SkipArgs &args,
+                                                     FptCudaPrimaryHit *hits, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(skip_primary_kernel<FPT_KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(skip_smem_bytes()));
+        attr = true;
+    }
+    const uint32_t warps = (W * H + 31u) / 32u;
+    const uint32_t blocks = (warps + kSkipWarps - 1u) / kSkipWarps;
+    skip_primary_kernel<FPT_KIND><<<blocks, 32 * kSkipWarps, skip_smem_bytes(), st>>>(scene, args, hits);
     return cudaGetLastError();
 }
 #if FPT_KIND == 0

@@ -1,0 +1,322 @@
+// skip.cuh -- surrogate-skip march: learned step proposals, certified by the exact DE.
+//
+// A ray at p with exact distance d_p = DE(p) asks the network for the
+// distance m at the look-ahead point p + 2 d_p dir and proposes the step
+// s = d_p + safety * m.  The exact DE at q = p + s dir decides:
+//   s <= d_p + DE(q)   the balls of radius d_p around p and DE(q) around q
+//                      hold no surface and overlap, so [p, q] is free:
+//                      the ray moves to q (one exact evaluation for s)
+//   otherwise          plain step 0.99 d_p (the reference march rule)
+// Every step is certified by the exact DE, so the surrogate only changes how
+// far a ray gets per evaluation, never what it hits.  When d_p falls below
+// the hand-over margin the exact march (march_update) finishes the ray.
+// Geometry lies inside the model's box: a ray that misses or leaves it is a
+// miss without further evaluation.
+//
+// The network runs on the tensor cores one warp at a time (32 rows), so the
+// loop is warp-synchronous: every iteration each lane adds one network row
+// and one exact evaluation.
+#pragma once
+
+#include "fpt_march.cuh"
+#include "mlp.cuh"
+#include "wavefront.cuh"
+
+namespace fpt {
+
+struct SkipArgs {
+    mlp::Model M;
+    float lo[3], hi[3];          // the model's box (all geometry inside)
+    float margin;                // hand over to the exact march below this distance
+    float safety;                // scale of the predicted distance in a proposal
+    uint32_t max_iters;          // skip iterations per ray before hand-over
+    unsigned long long *stats;   // kSkipStats counters or null
+};
+
+enum SkipStat : int { SK_ROWS = 0, SK_FORWARDS = 1, SK_EXACT = 2, SK_ACCEPT = 3, SK_REJECT = 4, SK_ESCAPE = 5, SK_HANDOVER = 6,
+                      SK_DIST = 7, kSkipStats = 8 };
+
+constexpr int kSkipWarps = 8;
+inline size_t skip_smem_bytes() { return ((sizeof(mlp::SmemWeights) + 127) & ~size_t(127)) + kSkipWarps * sizeof(mlp::WarpForward); }
+
+// Forward slab test: [tn, tf] of the ray inside the box, tn >= 0.
+__device__ __forceinline__ bool box_span(const SkipArgs &A, float3 p, float3 d, float &tn, float &tf) {
+    tn = 0.0f;
+    tf = 3.0e38f;
+    const float pv[3] = {p.x, p.y, p.z}, dv[3] = {d.x, d.y, d.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (dv[a] != 0.0f) {
+            float inv = 1.0f / dv[a];
+            float t0 = (A.lo[a] - pv[a]) * inv, t1 = (A.hi[a] - pv[a]) * inv;
+            tn = fmaxf(tn, fminf(t0, t1));
+            tf = fminf(tf, fmaxf(t0, t1));
+        } else if (pv[a] < A.lo[a] || pv[a] > A.hi[a]) {
+            return false;
+        }
+    }
+    return tf >= tn;
+}
+
+enum SkipPhase : int { SP_IDLE = 0, SP_EXACT = 1, SP_PROPOSE = 2 };
+
+struct SkipLane {
+    float3 origin, dir;   // job start and direction
+    float t;              // advance along dir from origin
+    float t_exit;         // box exit (advance)
+    float d;              // exact distance at origin + t dir (SP_PROPOSE)
+    int phase;
+    uint32_t iters;
+};
+
+// Starts a lane on a ray: clips to the box.  Returns false when the ray
+// never meets the box (a miss; t is left at 0).
+__device__ __forceinline__ bool skip_begin(SkipLane &L, const SkipArgs &A, float3 origin, float3 dir) {
+    L.origin = origin;
+    L.dir = dir;
+    L.t = 0.0f;
+    L.iters = 0;
+    L.d = 0.0f;
+    float tn, tf;
+    if (!box_span(A, origin, dir, tn, tf)) { L.phase = SP_IDLE; return false; }
+    L.t = tn;
+    L.t_exit = tf;
+    L.phase = SP_EXACT;
+    return true;
+}
+
+enum SkipOutcome : int { SO_CONTINUE = 0, SO_HANDOVER = 1, SO_ESCAPE = 2 };
+
+// One warp-synchronous iteration for all 32 lanes (every lane must call it;
+// lanes with phase SP_IDLE only lend their network row).
+template <int KIND>
+__device__ __forceinline__ int skip_step(SkipLane &L, const DeviceScene &S, const SkipArgs &A, const mlp::SmemWeights &sw,
+                                         mlp::WarpForward &wf, int lane, uint32_t &c_rows, uint32_t &c_fwd, uint32_t &c_exact,
+                                         uint32_t &c_acc, uint32_t &c_rej) {
+    const unsigned FULL = 0xffffffffu;
+    const bool propose = L.phase == SP_PROPOSE;
+    float3 p = L.origin + L.dir * L.t;
+    float m = 0.0f;
+    if (__any_sync(FULL, propose)) {
+        float3 q0 = propose ? p + L.dir * (2.0f * L.d) : p;
+        float u[3] = {(q0.x - A.M.center[0]) * A.M.inv_half[0], (q0.y - A.M.center[1]) * A.M.inv_half[1],
+                      (q0.z - A.M.center[2]) * A.M.inv_half[2]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) u[k] = fminf(fmaxf(u[k], -4.0f), 4.0f);
+        m = mlp::forward32(sw, wf, u, lane) * A.M.label_scale;
+        if (lane == 0) ++c_fwd;
+        if (propose) ++c_rows;
+    }
+    if (L.phase == SP_IDLE) return SO_CONTINUE;
+    bool cand = false;
+    float s = 0.0f;
+    if (propose) {
+        s = L.d + A.safety * fmaxf(m, 0.0f);
+        if (s > 1.25f * L.d && isfinite(s)) {
+            cand = true;
+        } else {   // no useful proposal: the plain step
+            L.t += 0.99f * L.d;
+            L.phase = SP_EXACT;
+        }
+    }
+    const float3 e_pt = L.origin + L.dir * (cand ? L.t + s : L.t);
+    const float de = scene_eval<KIND>(S, e_pt, EV_MAP).d;
+    ++c_exact;
+    if (cand) {
+        if (s <= L.d + de && isfinite(de)) {
+            L.t += s;
+            L.d = de;
+            ++c_acc;
+        } else {
+            L.t += 0.99f * L.d;
+            L.phase = SP_EXACT;
+            ++c_rej;
+        }
+    } else {
+        L.d = de;
+        L.phase = SP_PROPOSE;
+    }
+    if (L.t >= L.t_exit) return SO_ESCAPE;
+    if (L.phase == SP_PROPOSE && (!isfinite(L.d) || fabsf(L.d) < A.margin)) return SO_HANDOVER;
+    if (++L.iters >= A.max_iters) return SO_HANDOVER;
+    return SO_CONTINUE;
+}
+
+__device__ __forceinline__ void skip_flush_stats(const SkipArgs &A, int lane, uint32_t rows, uint32_t fwd, uint32_t exact,
+                                                 uint32_t acc, uint32_t rej, uint32_t esc, uint32_t hand) {
+    if (!A.stats) return;
+    uint32_t v[7] = {rows, fwd, exact, acc, rej, esc, hand};
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        uint32_t s = v[k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && s) atomicAdd(A.stats + k, (unsigned long long)s);
+    }
+}
+
+// Wavefront pass: advances the path rays of q_march[cur] and the shadow
+// rays of q_shadow[cur] before the exact march kernel takes them.  Path rays
+// move R.pos; escapes set PF_ESCAPED (the march kernel then classifies them
+// as misses without evaluating).  Shadow rays keep their advance in
+// normal.w; escapes set dir.w = 1 (unoccluded).  Jobs are taken with
+// per-lane regeneration from counter C_SKIP.
+template <int KIND>
+__global__ void __launch_bounds__(32 * kSkipWarps, 2) skip_march_kernel(WaveParams W, int cur, SkipArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    mlp::SmemWeights &sw = *reinterpret_cast<mlp::SmemWeights *>(smem_raw);
+    mlp::WarpForward *wf_all =
+        reinterpret_cast<mlp::WarpForward *>(smem_raw + ((sizeof(mlp::SmemWeights) + 127) & ~size_t(127)));
+    const DeviceScene &S = *W.scene;
+    const uint32_t n_path = W.counters[C_MARCH0 + cur];
+    const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
+    if (total == 0u) return;
+    mlp::load_weights(sw, A.M);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    mlp::WarpForward &wf = wf_all[warp];
+    const unsigned FULL = 0xffffffffu;
+    SkipLane L;
+    L.phase = SP_IDLE;
+    bool retired = false;
+    uint32_t job = 0;
+    bool shadow = false;
+    uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
+    uint32_t c_primary = 0, c_secondary = 0, c_shadow = 0;
+    uint32_t bounce = 0;
+    while (true) {
+        // Refill idle lanes (one atomic per warp); rays that miss the box are
+        // resolved at once and the lane draws again.
+        for (int tries = 0; tries < 4; ++tries) {
+            const bool need = L.phase == SP_IDLE && !retired;
+            unsigned ballot = __ballot_sync(FULL, need);
+            if (!ballot) break;
+            uint32_t leader = __ffs(ballot) - 1, base = 0;
+            if (lane == uint32_t(leader)) base = atomicAdd(&W.counters[C_SKIP], (unsigned)__popc(ballot));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
+                if (idx >= total) {
+                    retired = true;
+                } else {
+                    shadow = idx >= n_path;
+                    float3 o, d;
+                    if (!shadow) {
+                        job = W.q_march[cur][idx];
+                        const PathRec &R = W.paths[job];
+                        o = mk3(R.pos.x, R.pos.y, R.pos.z);
+                        d = mk3(R.dir.x, R.dir.y, R.dir.z);
+                        bounce = fbits(R.color.w) & 0xffu;
+                    } else {
+                        job = idx - n_path;
+                        const ShadowJob &J = W.q_shadow[cur][job];
+                        o = mk3(J.origin.x, J.origin.y, J.origin.z) + mk3(J.normal.x, J.normal.y, J.normal.z) * 0.001f;
+                        d = mk3(J.dir.x, J.dir.y, J.dir.z);
+                    }
+                    if (!skip_begin(L, A, o, d)) {
+                        ++c_esc;
+                        if (!shadow) W.paths[job].color.w = bitsf(fbits(W.paths[job].color.w) | PF_ESCAPED);
+                        else W.q_shadow[cur][job].dir.w = 1.0f;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(FULL, L.phase != SP_IDLE)) {
+            if (__all_sync(FULL, retired)) break;
+            continue;
+        }
+        const int out = skip_step<KIND>(L, S, A, sw, wf, lane, c_rows, c_fwd, c_exact, c_acc, c_rej);
+        if (L.phase != SP_IDLE) {
+            if (shadow) ++c_shadow; else if (bounce == 0u) ++c_primary; else ++c_secondary;
+        }
+        if (L.phase != SP_IDLE && out != SO_CONTINUE) {
+            if (out == SO_ESCAPE) ++c_esc; else ++c_hand;
+            if (!shadow) {
+                PathRec &R = W.paths[job];
+                float3 p = L.origin + L.dir * L.t;
+                R.pos = make_float4(p.x, p.y, p.z, R.pos.w);
+                if (out == SO_ESCAPE) R.color.w = bitsf(fbits(R.color.w) | PF_ESCAPED);
+            } else {
+                ShadowJob &J = W.q_shadow[cur][job];
+                J.normal.w = L.t;
+                if (out == SO_ESCAPE) J.dir.w = 1.0f;
+            }
+            L.phase = SP_IDLE;
+        }
+    }
+    skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
+    if (W.profile) {
+        uint32_t v[3] = {c_primary, c_secondary, c_shadow};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            uint32_t s = v[k];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+            if (lane == 0 && s) atomicAdd(W.profile + k, (unsigned long long)s);
+        }
+    }
+}
+
+// Primary rays with the surrogate skip in front of the exact march (the
+// counterpart of trace_primary_kernel): per pixel distance, normal, exact
+// evaluations (skip + march) and hit flag.
+template <int KIND>
+__global__ void __launch_bounds__(32 * kSkipWarps, 2) skip_primary_kernel(const DeviceScene *scene, SkipArgs A,
+                                                                          FptCudaPrimaryHit *hits) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    mlp::SmemWeights &sw = *reinterpret_cast<mlp::SmemWeights *>(smem_raw);
+    mlp::WarpForward *wf_all =
+        reinterpret_cast<mlp::WarpForward *>(smem_raw + ((sizeof(mlp::SmemWeights) + 127) & ~size_t(127)));
+    const DeviceScene &S = *scene;
+    mlp::load_weights(sw, A.M);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    mlp::WarpForward &wf = wf_all[warp];
+    const uint32_t pixels = S.width * S.height;
+    uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
+    for (uint32_t base = (blockIdx.x * kSkipWarps + warp) * 32u; base < pixels; base += gridDim.x * kSkipWarps * 32u) {
+        const uint32_t i = base + lane;
+        const bool valid = i < pixels;
+        const uint32_t gx = valid ? i % S.width : 0u, gy = valid ? i / S.width : 0u;
+        float2 uv = screen_uv(gx, gy, S);
+        PathRng rng;
+        rng.init(false, 0u, 0u, 0u, uv.x, uv.y);
+        float3 rp = mk3(0.f), dr = mk3(0.f, 0.f, 1.f);
+        bool ray = valid && camera_ray(S, uv, rng, false, rp, dr);
+        SkipLane L;
+        L.phase = SP_IDLE;
+        bool escaped = false;
+        uint32_t exact0 = c_exact;
+        if (ray && !skip_begin(L, A, rp, dr)) escaped = true;
+        while (__any_sync(0xffffffffu, L.phase != SP_IDLE)) {
+            int out = skip_step<KIND>(L, S, A, sw, wf, lane, c_rows, c_fwd, c_exact, c_acc, c_rej);
+            if (L.phase != SP_IDLE && out != SO_CONTINUE) {
+                if (out == SO_ESCAPE) { escaped = true; ++c_esc; } else ++c_hand;
+                L.phase = SP_IDLE;
+            }
+        }
+        if (!valid) continue;
+        FptCudaPrimaryHit h;
+        h.distance = 0.0f; h.normal[0] = h.normal[1] = h.normal[2] = 0.0f; h.steps = 0; h.hit = 0;
+        if (ray) {
+            if (escaped) {
+                h.distance = S.render[4];
+                h.steps = c_exact - exact0;
+            } else {
+                float3 start = L.origin + L.dir * L.t;
+                March m = march_loop<KIND>(S, start, dr, int(S.render[1]), S.render[3], 0.0002f);
+                float travel = len3(m.pos - rp);
+                bool hit = m.found && isfinite(travel) && travel < S.render[4] * 0.99f;
+                h.distance = travel;
+                h.steps = uint32_t(m.steps) + (c_exact - exact0);
+                h.hit = hit ? 1u : 0u;
+                if (hit) {
+                    float3 n = normal_direct<KIND>(m.pos, S);
+                    h.normal[0] = n.x; h.normal[1] = n.y; h.normal[2] = n.z;
+                }
+            }
+        }
+        hits[i] = h;
+    }
+    skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
+}
+
+}  // namespace fpt

@@ -27,7 +27,9 @@
 
 namespace fpt {
 
-enum PathFlags : uint32_t { PF_DONE = 1u << 8, PF_INVISIBLE = 1u << 9, PF_VALID = 1u << 10 };
+// PF_ESCAPED: the surrogate-skip pass found the ray leaving the geometry's
+// box; the march classifies it as a miss without evaluating.
+enum PathFlags : uint32_t { PF_DONE = 1u << 8, PF_INVISIBLE = 1u << 9, PF_VALID = 1u << 10, PF_ESCAPED = 1u << 11 };
 
 struct alignas(16) PathRec {
     float4 pos;     // xyz march origin or hit point, w side
@@ -40,13 +42,13 @@ struct alignas(16) PathRec {
 
 struct alignas(16) ShadowJob {
     float4 origin;  // xyz hit point, w path index bits
-    float4 normal;  // xyz normal the ray leaves along (offset 0.001)
-    float4 dir;     // xyz light direction
+    float4 normal;  // xyz normal the ray leaves along (offset 0.001), w advance made by the skip pass
+    float4 dir;     // xyz light direction, w 1 when the skip pass found the ray leaving the geometry's box
     float4 contrib; // xyz light added when the ray escapes
 };
 
 // Device counters of one wave.
-enum Counter : uint32_t { C_MARCH0 = 0, C_MARCH1 = 1, C_SHADOW0 = 2, C_SHADOW1 = 3, C_SHADE = 4, C_HEAD = 5, C_COUNT = 8 };
+enum Counter : uint32_t { C_MARCH0 = 0, C_MARCH1 = 1, C_SHADOW0 = 2, C_SHADOW1 = 3, C_SHADE = 4, C_HEAD = 5, C_SKIP = 6, C_COUNT = 8 };
 
 struct WaveParams {
     const DeviceScene *scene;
@@ -183,9 +185,17 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
                     job.shadow = false;
                     const PathRec &R = W.paths[job.path];
                     float4 pos = R.pos, dir = R.dir;
-                    job.bounce = fbits(R.color.w) & 0xffu;
+                    const uint32_t st = fbits(R.color.w);
+                    job.bounce = st & 0xffu;
                     int ni = job.bounce == 0u ? int(S.render[1]) : int(S.render[1] / (S.render[5] * 2.0f + 1.0f));
-                    active = march_begin(m, S, mk3(pos.x, pos.y, pos.z), mk3(dir.x, dir.y, dir.z), ni, S.render[3], 0.0002f);
+                    float3 o = mk3(pos.x, pos.y, pos.z), dv = mk3(dir.x, dir.y, dir.z);
+                    if (st & PF_ESCAPED) {   // a miss: end beyond the far limit
+                        active = false;
+                        m.steps = 0;
+                        m.pos = o + dv * (S.render[4] + len3(o - cam) + 1.0f);
+                    } else {
+                        active = march_begin(m, S, o, dv, ni, S.render[3], 0.0002f);
+                    }
                     pending = !active;
                 } else {
                     const ShadowJob &J = qs[idx - n_path];
@@ -194,8 +204,15 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
                     job.shadow = true;
                     job.contrib = J.contrib;
                     job.rp0 = mk3(o.x, o.y, o.z);
-                    float3 start = job.rp0 + mk3(nn.x, nn.y, nn.z) * 0.001f;
-                    active = march_begin(m, S, start, mk3(d.x, d.y, d.z), int(S.render[1]), S.render[3], 0.0002f);
+                    float3 dv = mk3(d.x, d.y, d.z);
+                    if (d.w == 1.0f) {   // unoccluded: end beyond the far limit
+                        active = false;
+                        m.steps = 0;
+                        m.pos = job.rp0 + dv * (S.render[4] * 1.01f + 1.0f);
+                    } else {
+                        float3 start = job.rp0 + mk3(nn.x, nn.y, nn.z) * 0.001f + dv * nn.w;
+                        active = march_begin(m, S, start, dv, int(S.render[1]), S.render[3], 0.0002f);
+                    }
                     pending = !active;
                 }
             }
@@ -470,6 +487,7 @@ static __global__ void reset_counters_kernel(uint32_t *counters, int next) {
         counters[C_SHADOW0 + next] = 0u;
         counters[C_SHADE] = 0u;
         counters[C_HEAD] = 0u;
+        counters[C_SKIP] = 0u;
     }
 }
 

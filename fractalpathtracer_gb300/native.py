@@ -22,7 +22,8 @@ EXPORTED = [
     "fpt_metal_device_name", "fpt_test_voxel_dda", "fpt_test_async_stitch_context", "fpt_test_typed_soa",
     "fpt_metal_preview", "fpt_cuda_trace_primary", "fpt_cuda_render", "fpt_cuda_sample_distance",
     "fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render",
-    "fpt_cuda_voxel_build_static",
+    "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
+    "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
 ]
 
 

@@ -19,6 +19,24 @@ class FptCudaVoxelHit(C.Structure):
                 ("shadow_steps", C.c_uint32), ("lit", C.c_uint32)]
 
 
+class FptCudaMlpConfig(C.Structure):
+    _fields_ = [("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3), ("points", C.c_uint32),
+                ("near_fraction", C.c_float), ("near_band", C.c_float), ("batch", C.c_uint32), ("steps", C.c_uint32),
+                ("lr", C.c_float), ("overestimate_weight", C.c_float), ("seed", C.c_uint32), ("_reserved", C.c_uint32 * 4)]
+
+
+class FptCudaMlpStats(C.Structure):
+    _fields_ = [("loss_first", C.c_float), ("loss_last", C.c_float), ("data_ms", C.c_double), ("train_ms", C.c_double),
+                ("params", C.c_uint32), ("steps", C.c_uint32), ("label_scale", C.c_float), ("near_points", C.c_uint32)]
+
+
+class FptCudaSkipStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("rows", "forwards", "exact_evals", "accepted", "rejected", "escaped",
+                                          "handed_over", "reserved")]
+
+
+MLP_PARAMS = 19777
+
 VOXEL_HIT_DTYPE = np.dtype([("t", np.float32), ("cell", np.uint32), ("normal_axis", np.uint32), ("steps", np.uint32),
                             ("shadow_steps", np.uint32), ("lit", np.uint32)])
 
@@ -35,8 +53,17 @@ def declare(L: C.CDLL) -> None:
                                         P(C.c_double)] + err
     L.fpt_cuda_voxel_build_static.argtypes = [cfg, ext, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
                                               C.c_size_t, P(FptCudaVoxelInfo)] + err
+    fp = P(C.c_float)
+    L.fpt_cuda_mlp_create.argtypes = [cfg, ext, P(FptCudaMlpConfig), P(C.c_uint64), P(FptCudaMlpStats)] + err
+    L.fpt_cuda_mlp_destroy.argtypes = [C.c_uint64]
+    L.fpt_cuda_mlp_predict.argtypes = [C.c_uint64, fp, C.c_size_t, fp] + err
+    L.fpt_cuda_mlp_get_params.argtypes = [C.c_uint64, fp, C.c_size_t] + err
+    L.fpt_cuda_mlp_set_params.argtypes = [C.c_uint64, fp, C.c_size_t] + err
+    L.fpt_cuda_mlp_gradients.argtypes = [C.c_uint64, fp, C.c_size_t, C.c_float, fp, C.c_size_t, fp] + err
+    L.fpt_cuda_skip_stats.argtypes = [P(FptCudaSkipStats)]
     for name in ("fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render",
-                 "fpt_cuda_voxel_build_static"):
+                 "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
+                 "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats"):
         getattr(L, name).restype = C.c_int
 
 
@@ -113,3 +140,79 @@ def voxel_build_static(cfg, ext, device_table: int, table_len: int, device_occup
                                              table_len, device_occupancy, device_distance, cell_capacity, C.byref(info),
                                              e, len(e)), e)
     return {k: getattr(info, k) for k, _ in FptCudaVoxelInfo._fields_}
+
+
+# ---------------------------------------------------------------- learned surrogate
+def mlp_config(bounds_min, bounds_max, points=1 << 24, near_fraction=0.5, near_band=0.05, batch=16384, steps=2000,
+               lr=2e-3, overestimate_weight=10.0, seed=1) -> FptCudaMlpConfig:
+    mc = FptCudaMlpConfig()
+    for k in range(3):
+        mc.bounds_min[k] = float(bounds_min[k])
+        mc.bounds_max[k] = float(bounds_max[k])
+    mc.points, mc.near_fraction, mc.near_band = int(points), float(near_fraction), float(near_band)
+    mc.batch, mc.steps, mc.lr = int(batch), int(steps), float(lr)
+    mc.overestimate_weight, mc.seed = float(overestimate_weight), int(seed)
+    return mc
+
+
+def mlp_create(cfg, ext, mc: FptCudaMlpConfig):
+    """Trains a surrogate on the GPU; returns (handle, stats dict)."""
+    from .native import lib
+    h = C.c_uint64()
+    st = FptCudaMlpStats()
+    e = _err()
+    _check(lib().fpt_cuda_mlp_create(C.byref(cfg), C.byref(ext) if ext is not None else None, C.byref(mc), C.byref(h),
+                                     C.byref(st), e, len(e)), e)
+    return h.value, {k: getattr(st, k) for k, _ in FptCudaMlpStats._fields_}
+
+
+def mlp_destroy(handle: int) -> None:
+    from .native import lib
+    lib().fpt_cuda_mlp_destroy(handle)
+
+
+def _f32(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def mlp_predict(handle: int, points) -> np.ndarray:
+    from .native import lib
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+    out = np.zeros(len(pts), np.float32)
+    e = _err()
+    _check(lib().fpt_cuda_mlp_predict(handle, _f32(pts), len(pts), _f32(out), e, len(e)), e)
+    return out
+
+
+def mlp_get_params(handle: int) -> np.ndarray:
+    from .native import lib
+    out = np.zeros(MLP_PARAMS, np.float32)
+    e = _err()
+    _check(lib().fpt_cuda_mlp_get_params(handle, _f32(out), len(out), e, len(e)), e)
+    return out
+
+
+def mlp_set_params(handle: int, params) -> None:
+    from .native import lib
+    p = np.ascontiguousarray(params, np.float32)
+    e = _err()
+    _check(lib().fpt_cuda_mlp_set_params(handle, _f32(p), len(p), e, len(e)), e)
+
+
+def mlp_gradients(handle: int, points, overestimate_weight=10.0):
+    """(gradients[19777], mean loss) of the asymmetric loss over labelled xyzw points."""
+    from .native import lib
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+    g = np.zeros(MLP_PARAMS, np.float32)
+    loss = C.c_float()
+    e = _err()
+    _check(lib().fpt_cuda_mlp_gradients(handle, _f32(pts), len(pts), overestimate_weight, _f32(g), len(g), C.byref(loss), e,
+                                        len(e)), e)
+    return g, loss.value
+
+
+def skip_stats() -> dict:
+    from .native import lib
+    st = FptCudaSkipStats()
+    lib().fpt_cuda_skip_stats(C.byref(st))
+    return {k: getattr(st, k) for k, _ in FptCudaSkipStats._fields_ if k != "reserved"}

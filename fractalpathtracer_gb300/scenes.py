@@ -285,6 +285,34 @@ def mandelbox_path(width: int = 1920, height: int = 1080, spp: int = 16, bounces
     return _fractal_path(mandelbox_ext(), width, height, spp, bounces, seed, (0.0, 1.5, -7.0), (0.0, 0.0, 0.0), 1e-4 / 7.0)
 
 
+# Boxes holding all of each surrogate scene's surface (the power-8 Mandelbulb
+# reaches |x| ~ 1.11, the scale -1.5 Mandelbox |x| ~ 2.01): the skip march
+# treats rays leaving them as misses.
+SURROGATE_BOXES = {
+    "mandelbulb": ((-1.25, -1.25, -1.25), (1.25, 1.25, 1.25)),
+    "mandelbox": ((-2.25, -2.25, -2.25), (2.25, 2.25, 2.25)),
+}
+
+
+def random_mlp_params(seed: int = 0, out_scale: float = 0.3) -> np.ndarray:
+    """He-uniform parameters in the surrogate's layout (W0 padding columns zero), for parity tests."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(19777, np.float32)
+    off = 0
+    for layer in range(4):
+        k, fan = (112, 99) if layer == 0 else (64, 64)
+        w = rng.uniform(-1, 1, (64, k)) * np.sqrt(6.0 / fan)
+        if layer == 0:
+            w[:, 99:] = 0.0
+        p[off:off + 64 * k] = w.ravel()
+        off += 64 * k
+        p[off:off + 64] = rng.uniform(-0.1, 0.1, 64)
+        off += 64
+    p[off:off + 64] = rng.uniform(-out_scale, out_scale, 64)
+    p[off + 64] = 0.05
+    return p
+
+
 def voxel_mandelbox(resolution: int = 1024, width: int = 1920, height: int = 1080):
     """Mandelbox (scale -1.5, 12 iterations, min radius 0.5, fold limit 1) voxelized over [-4, 4]^3;
     primary + one shadow ray per pixel through the occupancy bricks."""

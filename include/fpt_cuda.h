@@ -747,6 +747,78 @@ int fpt_cuda_voxel_build_static(const struct FptRenderConfig *config,
                                 char *error,
                                 size_t error_len);
 
+/* ---- Learned distance surrogate (no counterpart in the reference) ----
+ * Network: 3-D point -> 99 Fourier features (the point normalised to the
+ * box, sin/cos of pi 2^(6k/15) u for k < 16) -> 4 x 64 SiLU -> 1 distance;
+ * BF16 weights and activations, FP32 accumulation, FP32 master copy.
+ * Parameter layout (floats): W0[64][112] (columns 99..111 zero), b0[64],
+ * W1[64][64], b1, W2, b2, W3, b3, W4[64], b4 -- 19777 values. */
+struct FptCudaMlpConfig {
+    float bounds_min[3];         /* box of the training points; all geometry must lie inside */
+    float bounds_max[3];
+    uint32_t points;             /* training points, labelled by the scene's exact DE */
+    float near_fraction;         /* share drawn within near_band of the surface */
+    float near_band;             /* world units (0: 0.05) */
+    uint32_t batch;              /* rows per optimisation step */
+    uint32_t steps;              /* Adam steps (0: initialise only) */
+    float lr;                    /* peak learning rate, cosine decay to 2% (0: 2e-3) */
+    float overestimate_weight;   /* loss weight of overestimates (0: 10) */
+    uint32_t seed;
+    uint32_t _reserved[4];
+};
+
+struct FptCudaMlpStats {
+    float loss_first;            /* mean loss of the first batch */
+    float loss_last;             /* mean loss of the last batch */
+    double data_ms;              /* training-data generation */
+    double train_ms;             /* optimisation */
+    uint32_t params;
+    uint32_t steps;
+    float label_scale;           /* network output x label_scale = distance */
+    uint32_t near_points;
+};
+
+/* Counters of the last render or primary trace that used the surrogate
+ * skip (FPT_CUDA_SURROGATE_SKIP). */
+struct FptCudaSkipStats {
+    uint64_t rows;               /* network rows used for proposals */
+    uint64_t forwards;           /* warp-wide network passes (32 rows each) */
+    uint64_t exact_evals;        /* exact DE evaluations inside the skip pass */
+    uint64_t accepted;           /* proposals certified by the exact DE */
+    uint64_t rejected;           /* proposals refused (plain step taken) */
+    uint64_t escaped;            /* rays found leaving the box (misses) */
+    uint64_t handed_over;        /* rays handed to the exact march */
+    uint64_t reserved;
+};
+
+/* Generates the training data on the GPU, trains the network with the
+ * library's own BF16 tensor-core forward/backward kernels and Adam, and
+ * returns a handle.  The scene (config + ext) supplies the exact DE. */
+int fpt_cuda_mlp_create(const struct FptRenderConfig *config,
+                        const struct FptCudaSceneExt *ext,
+                        const struct FptCudaMlpConfig *mlp,
+                        uint64_t *model,
+                        struct FptCudaMlpStats *stats,
+                        char *error,
+                        size_t error_len);
+int fpt_cuda_mlp_destroy(uint64_t model);
+/* Network distance at n xyzw points (w ignored). */
+int fpt_cuda_mlp_predict(uint64_t model, const float *points_xyzw, size_t n, float *distances, char *error, size_t error_len);
+int fpt_cuda_mlp_get_params(uint64_t model, float *params, size_t len, char *error, size_t error_len);
+int fpt_cuda_mlp_set_params(uint64_t model, const float *params, size_t len, char *error, size_t error_len);
+/* Gradients of the mean asymmetric loss over n labelled points (xyz, w =
+ * target distance) with the current parameters; no update. */
+int fpt_cuda_mlp_gradients(uint64_t model,
+                           const float *points_xyzw,
+                           size_t n,
+                           float overestimate_weight,
+                           float *gradients,
+                           size_t len,
+                           float *loss,
+                           char *error,
+                           size_t error_len);
+int fpt_cuda_skip_stats(struct FptCudaSkipStats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,10 @@ def lib() -> C.CDLL:
         L.oracle_dda_contract.restype = C.c_uint32
         L.oracle_float_to_half.argtypes = [C.c_float]
         L.oracle_float_to_half.restype = C.c_uint16
+        fp = P(C.c_float)
+        L.oracle_mlp_forward.argtypes = [fp, fp, fp, C.c_float, fp, C.c_size_t, C.c_int, P(C.c_double)]
+        L.oracle_mlp_gradients.argtypes = [fp, fp, fp, C.c_float, fp, C.c_size_t, C.c_float, C.c_int, P(C.c_double),
+                                           P(C.c_double)]
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_max_threads.restype = C.c_int
         _lib = L
@@ -182,3 +186,36 @@ def dda_contract():
 
 def float_to_half(values):
     return np.array([lib().oracle_float_to_half(float(v)) for v in np.asarray(values, np.float32)], np.uint16)
+
+
+def _mlp_frame(bounds_min, bounds_max):
+    lo = np.asarray(bounds_min, np.float32)
+    hi = np.asarray(bounds_max, np.float32)
+    center = (np.float32(0.5) * (lo + hi)).astype(np.float32)
+    half = (np.float32(0.5) * (hi - lo)).astype(np.float32)
+    inv_half = (np.float32(1.0) / half).astype(np.float32)
+    return center, inv_half, np.float32(half.max())
+
+
+def mlp_forward(params, bounds_min, bounds_max, points, emulate_bf16=True):
+    """FP64 network output (distance units) at xyzw points; the frame follows the CUDA model's box."""
+    center, inv_half, scale = _mlp_frame(bounds_min, bounds_max)
+    p = np.ascontiguousarray(params, np.float32)
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+    out = np.zeros(len(pts), np.float64)
+    lib().oracle_mlp_forward(_p(p, C.c_float), _p(center, C.c_float), _p(inv_half, C.c_float), float(scale),
+                             _p(pts, C.c_float), len(pts), int(emulate_bf16), _p(out, C.c_double))
+    return out
+
+
+def mlp_gradients(params, bounds_min, bounds_max, points, overestimate_weight=10.0, emulate_bf16=True):
+    """FP64 gradients (19777) and mean loss of the asymmetric loss over labelled xyzw points."""
+    center, inv_half, scale = _mlp_frame(bounds_min, bounds_max)
+    p = np.ascontiguousarray(params, np.float32)
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+    g = np.zeros(len(p), np.float64)
+    loss = np.zeros(1, np.float64)
+    lib().oracle_mlp_gradients(_p(p, C.c_float), _p(center, C.c_float), _p(inv_half, C.c_float), float(scale),
+                               _p(pts, C.c_float), len(pts), float(overestimate_weight), int(emulate_bf16),
+                               _p(g, C.c_double), _p(loss, C.c_double))
+    return g, float(loss[0])

@@ -2182,3 +2182,152 @@ uint32_t oracle_dda_contract(void) {
 uint16_t oracle_float_to_half(float f) { return float_to_half_rne(f); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- learned surrogate
+// FP64 restatement of the surrogate network (no counterpart in the
+// reference): features, forward pass and the gradients of the mean
+// asymmetric squared loss.  With `emulate` set, values are rounded to BF16
+// where the CUDA kernels store BF16 (weights, features, pre-activations,
+// activations and deltas), so the remaining differences come from the
+// accumulation order and the hardware tanh/sin/cos approximations.
+namespace mlp_ref {
+
+constexpr int kFreq = 16, kIn = 99, kInPad = 112, kHid = 64;
+constexpr int kW0 = 0, kB0 = kW0 + kHid * kInPad, kW1 = kB0 + kHid, kB1 = kW1 + kHid * kHid, kW2 = kB1 + kHid,
+              kB2 = kW2 + kHid * kHid, kW3 = kB2 + kHid, kB3 = kW3 + kHid * kHid, kW4 = kB3 + kHid, kB4 = kW4 + kHid,
+              kParams = kB4 + 1;
+const int kWOff[4] = {kW0, kW1, kW2, kW3}, kBOff[4] = {kB0, kB1, kB2, kB3}, kK[4] = {kInPad, kHid, kHid, kHid};
+
+double bf16(double v, bool emulate) {
+    if (!emulate) return v;
+    float f = float(v);
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u += 0x7fffu + ((u >> 16) & 1u);   // round to nearest even
+    u &= 0xffff0000u;
+    std::memcpy(&f, &u, 4);
+    return double(f);
+}
+double sigmoid(double z) { return 1.0 / (1.0 + std::exp(-z)); }
+double silu(double z) { return z * sigmoid(z); }
+double silu_grad(double z) {
+    double s = sigmoid(z);
+    return s + z * s * (1.0 - s);
+}
+
+struct Net {
+    std::vector<double> p;   // parameters (weights rounded when emulating)
+    double center[3], inv_half[3], label_scale;
+    bool emulate;
+};
+
+Net make_net(const float *params, const float *center, const float *inv_half, float label_scale, bool emulate) {
+    Net n;
+    n.p.assign(params, params + kParams);
+    for (int l = 0; l < 4; ++l)
+        for (int i = 0; i < kHid * kK[l]; ++i) n.p[kWOff[l] + i] = bf16(n.p[kWOff[l] + i], emulate);
+    for (int j = 0; j < kHid; ++j) n.p[kW4 + j] = bf16(n.p[kW4 + j], emulate);
+    for (int k = 0; k < 3; ++k) { n.center[k] = center[k]; n.inv_half[k] = inv_half[k]; }
+    n.label_scale = label_scale;
+    n.emulate = emulate;
+    return n;
+}
+
+// u, then (sin, cos)(pi 2^(6k/15) u_i) for k < 16, i < 3; zero padding to 112.
+void features(const Net &n, const float *pt, double *x) {
+    double u[3];
+    for (int i = 0; i < 3; ++i) u[i] = double(float((pt[i] - float(n.center[i])) * float(n.inv_half[i])));
+    for (int i = 0; i < 3; ++i) x[i] = bf16(u[i], n.emulate);
+    for (int k = 0; k < kFreq; ++k) {
+        double f = 3.14159265358979323846 * std::exp2(6.0 * k / 15.0);
+        for (int i = 0; i < 3; ++i) {
+            x[3 + (k * 3 + i) * 2] = bf16(std::sin(f * u[i]), n.emulate);
+            x[3 + (k * 3 + i) * 2 + 1] = bf16(std::cos(f * u[i]), n.emulate);
+        }
+    }
+    for (int j = kIn; j < kInPad; ++j) x[j] = 0.0;
+}
+
+struct Trace {
+    double x[kInPad];
+    double z[4][kHid], h[4][kHid];
+    double out;
+};
+
+void forward(const Net &n, const float *pt, Trace &t) {
+    features(n, pt, t.x);
+    const double *in = t.x;
+    for (int l = 0; l < 4; ++l) {
+        for (int o = 0; o < kHid; ++o) {
+            double acc = 0.0;
+            for (int k = 0; k < kK[l]; ++k) acc += in[k] * n.p[kWOff[l] + o * kK[l] + k];
+            double z = acc + double(float(n.p[kBOff[l] + o]));
+            t.z[l][o] = bf16(z, n.emulate);
+            t.h[l][o] = bf16(silu(z), n.emulate);
+        }
+        in = t.h[l];
+    }
+    double out = n.p[kB4];
+    for (int j = 0; j < kHid; ++j) out += t.h[3][j] * n.p[kW4 + j];
+    t.out = out;
+}
+
+}  // namespace mlp_ref
+
+extern "C" {
+
+// Network output (distance units) at n xyzw points.
+void oracle_mlp_forward(const float *params, const float *center, const float *inv_half, float label_scale, const float *pts,
+                        size_t n, int emulate, double *out) {
+    mlp_ref::Net net = mlp_ref::make_net(params, center, inv_half, label_scale, emulate != 0);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < long(n); ++i) {
+        mlp_ref::Trace t;
+        mlp_ref::forward(net, pts + 4 * i, t);
+        out[i] = t.out * net.label_scale;
+    }
+}
+
+// Gradients of L = (1/n) sum_b w_b (out_b - y_b)^2, y_b = label_b / label_scale,
+// w_b = over_weight when out_b > y_b else 1 (the CUDA training loss).
+void oracle_mlp_gradients(const float *params, const float *center, const float *inv_half, float label_scale, const float *pts,
+                          size_t n, float over_weight, int emulate, double *grad, double *loss) {
+    using namespace mlp_ref;
+    Net net = make_net(params, center, inv_half, label_scale, emulate != 0);
+    std::vector<double> g(kParams, 0.0);
+    double total = 0.0;
+    const double inv_scale = double(1.0f / label_scale);
+    for (size_t b = 0; b < n; ++b) {
+        Trace t;
+        forward(net, pts + 4 * b, t);
+        const double y = double(float(pts[4 * b + 3] * float(inv_scale)));
+        const double e = t.out - y;
+        const double w = e > 0.0 ? double(over_weight) : 1.0;
+        total += w * e * e;
+        const double dout = 2.0 * w * e / double(n);
+        g[kB4] += dout;
+        double dz[kHid], dzn[kHid];
+        for (int j = 0; j < kHid; ++j) {
+            g[kW4 + j] += dout * t.h[3][j];
+            dz[j] = bf16(dout * net.p[kW4 + j] * silu_grad(t.z[3][j]), net.emulate);
+        }
+        for (int l = 3; l >= 0; --l) {
+            const double *in = l == 0 ? t.x : t.h[l - 1];
+            for (int o = 0; o < kHid; ++o) {
+                g[kBOff[l] + o] += dz[o];
+                for (int k = 0; k < kK[l]; ++k) g[kWOff[l] + o * kK[l] + k] += dz[o] * in[k];
+            }
+            if (l == 0) break;
+            for (int i = 0; i < kHid; ++i) {
+                double acc = 0.0;
+                for (int o = 0; o < kHid; ++o) acc += dz[o] * net.p[kWOff[l] + o * kHid + i];
+                dzn[i] = bf16(acc * silu_grad(t.z[l - 1][i]), net.emulate);
+            }
+            std::memcpy(dz, dzn, sizeof(dz));
+        }
+    }
+    for (int i = 0; i < kParams; ++i) grad[i] = g[i];
+    if (loss) *loss = total / double(n);
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+"""Learned distance surrogate on the GPU.
+
+* Forward pass and gradients of the BF16 tensor-core kernels against the FP64
+  oracle that rounds to BF16 where the kernels store BF16 (the remaining
+  differences: FP32 accumulation order, the hardware tanh/sin/cos, BF16
+  rounding-boundary flips).  Tolerances: forward |dy| <= 2e-3 * (max|y| + 0.1)
+  for 99% of points; per parameter block ||g - g_ref|| <= 2e-2 ||g_ref||.
+* Training on the GPU lowers the asymmetric loss by 10x and keeps
+  overestimates rare.
+* The skip march gives the same hits as the plain march: hit/miss
+  agreement >= 99.5% and hit-distance error versus the FP64 oracle within
+  the plain march's own 99th percentile (both within 5e-5 (1 + t)); it
+  reports the exact DE evaluations with the trained network, without it
+  (same march, zero network) and without the skip pass.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from fractalpathtracer_gb300 import native_ext as nx
+from fractalpathtracer_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+BULB_BOX = scenes.SURROGATE_BOXES["mandelbulb"]
+
+
+def _points(n, seed):
+    rng = np.random.default_rng(seed)
+    p = np.zeros((n, 4), np.float32)
+    p[:, :3] = rng.uniform(-1.2, 1.2, (n, 3))
+    p[:, 3] = rng.uniform(-0.05, 0.6, n)
+    return p
+
+
+@pytest.fixture(scope="module")
+def blank_model(native):
+    cfg, ext = scenes.mandelbulb_primary(8, 8)
+    mc = nx.mlp_config(*BULB_BOX, points=0, steps=0)
+    h, _ = nx.mlp_create(cfg, ext, mc)
+    yield h
+    nx.mlp_destroy(h)
+
+
+def test_forward_matches_oracle(blank_model):
+    params = scenes.random_mlp_params(11)
+    nx.mlp_set_params(blank_model, params)
+    back = nx.mlp_get_params(blank_model)
+    assert np.array_equal(back, params)
+    pts = _points(4096, 5)
+    y = nx.mlp_predict(blank_model, pts).astype(np.float64)
+    ref = oracle.mlp_forward(params, *BULB_BOX, pts, emulate_bf16=True)
+    err = np.abs(y - ref)
+    scale = np.abs(ref).max() + 0.1
+    print(f"forward: max|y| {np.abs(ref).max():.3f} p99 err {np.percentile(err, 99):.2e} max err {err.max():.2e}")
+    assert np.percentile(err, 99) <= 2e-3 * scale
+    assert err.max() <= 1e-2 * scale
+
+
+def test_gradients_match_oracle(blank_model):
+    params = scenes.random_mlp_params(12)
+    nx.mlp_set_params(blank_model, params)
+    pts = _points(1000, 6)   # not a multiple of the 128-row block: exercises the ragged tail
+    g, loss = nx.mlp_gradients(blank_model, pts, 10.0)
+    g_ref, loss_ref = oracle.mlp_gradients(params, *BULB_BOX, pts, 10.0, emulate_bf16=True)
+    assert abs(loss - loss_ref) <= 5e-3 * loss_ref
+    blocks = {"W0": (0, 7168), "b0": (7168, 7232), "W1": (7232, 11328), "b1": (11328, 11392), "W2": (11392, 15488),
+              "b2": (15488, 15552), "W3": (15552, 19648), "b3": (19648, 19712), "W4": (19712, 19776), "b4": (19776, 19777)}
+    for name, (a, b) in blocks.items():
+        d = np.linalg.norm(g[a:b] - g_ref[a:b])
+        r = np.linalg.norm(g_ref[a:b])
+        print(f"{name}: |g| {r:.3e} rel err {d / max(r, 1e-30):.2e}")
+        assert d <= 2e-2 * r + 1e-7, name
+    pad = g[:7168].reshape(64, 112)[:, 99:]
+    assert np.abs(pad).max() < 1e-3 * np.abs(g[:7168]).max()   # padding columns carry no real gradient
+
+
+@pytest.fixture(scope="module")
+def trained_bulb(native):
+    cfg, ext = scenes.mandelbulb_primary(8, 8)
+    mc = nx.mlp_config(*BULB_BOX, points=1 << 20, steps=800, batch=8192, lr=2e-3, seed=3)
+    h, stats = nx.mlp_create(cfg, ext, mc)
+    print("training:", stats)
+    yield h, stats
+    nx.mlp_destroy(h)
+
+
+def test_training_reduces_loss_and_underestimates(trained_bulb, native):
+    h, stats = trained_bulb
+    assert stats["near_points"] == (1 << 19)
+    assert stats["loss_last"] < 0.1 * stats["loss_first"], stats
+    cfg, ext = scenes.mandelbulb_primary(8, 8)
+    rng = np.random.default_rng(9)
+    pts = np.zeros((65536, 4), np.float32)
+    pts[:, :3] = rng.uniform(-1.25, 1.25, (65536, 3))
+    exact = native.sample_distance(cfg, ext, pts)[:, 0].astype(np.float64)
+    pred = nx.mlp_predict(h, pts).astype(np.float64)
+    err = pred - exact
+    over = (err > 0.02).mean()
+    under = (err < -0.02).mean()
+    print(f"held-out: mean |err| {np.abs(err).mean():.4f} over>0.02 {over:.4f} under<-0.02 {under:.4f}")
+    assert np.abs(err).mean() < 0.05
+    assert over < under + 0.01
+
+
+def _hits(native, cfg, ext):
+    hits, ms = native.trace_primary(cfg, ext)
+    return hits, ms
+
+
+def test_skip_march_keeps_hits(trained_bulb, native):
+    h, _ = trained_bulb
+    cfg, ext = scenes.mandelbulb_primary(320, 240)
+    plain, _ = _hits(native, cfg, ext)
+    ref = oracle.trace_primary(cfg, ext, fp64=True)
+
+    def run(model):
+        e = scenes.mandelbulb_primary(320, 240)[1]
+        e.surrogate = 1
+        e.surrogate_model = model
+        hits, _ = _hits(native, cfg, e)
+        return hits, nx.skip_stats()
+
+    skip, st = run(h)
+    # the same march without the network: a model whose output is zero
+    zero_cfg, zero_ext = scenes.mandelbulb_primary(8, 8)
+    z, _ = nx.mlp_create(zero_cfg, zero_ext, nx.mlp_config(*BULB_BOX, points=0, steps=0))
+    try:
+        nx.mlp_set_params(z, np.zeros(nx.MLP_PARAMS, np.float32))
+        nonet, st0 = run(z)
+    finally:
+        nx.mlp_destroy(z)
+    hit_r = ref[..., 5] > 0
+    rows = []
+    for name, g in (("plain", plain), ("skip", skip), ("no-network", nonet)):
+        hit_g = g["hit"] > 0
+        both = hit_g & hit_r
+        derr = np.abs(g["distance"][both] - ref[..., 0][both]) / (1 + ref[..., 0][both])
+        rows.append((name, (hit_g == hit_r).mean(), np.percentile(derr, 99), int(g["steps"].astype(np.int64).sum())))
+    for r in rows:
+        print("%-10s agree %.5f p99 dist err %.2e exact evals %d" % r)
+    print("skip stats:", st)
+    print("no-network stats:", st0)
+    (_, a0, e0, n0), (_, a1, e1, n1), (_, a2, e2, n2) = rows
+    assert a1 >= 0.995 and a2 >= 0.995
+    assert e1 <= 5e-5 and e1 <= 1.5 * e0 + 1e-6
+    assert e2 <= 5e-5
+    assert st["accepted"] > 0 and st["rows"] > 0
+    agree = ((skip["hit"] > 0) == (plain["hit"] > 0)).mean()
+    assert agree >= 0.995
