@@ -1,12 +1,15 @@
-"""Benchmark: Mpaths/s at 1920x1080, 16 spp, 4 bounces (power-8 Mandelbulb path tracing).
+"""Benchmark: Mpaths/s at 1920x1080, 16 spp, 4 bounces (power-8 Mandelbulb path tracing),
+surrogate-skip march vs plain march.
 
 One step = one full render of the frame (W*H*spp camera paths through all
-their bounces) by libfpt_cuda.so.  `value` is device throughput measured
-with CUDA events on the library's stream (scene resident in HBM); `e2e` is
-the same metric through the public C ABI call with host buffers (config
-upload and image readback inside the timed region).  The working set (one
-33 MB accumulation buffer) fits in L2, so L2 is flushed by writing a 256 MB
-buffer between timed steps.
+their bounces) by libfpt_cuda.so.  `value` is the surrogate-skip march's
+device throughput, measured with CUDA events on the library's stream (scene
+and trained network resident in HBM); the plain march is measured the same
+way beside it, and primary rays of both marches are compared for equal hit
+distance.  `e2e` is the same metric through the public C ABI call with host
+buffers (config upload and image readback inside the timed region).  The
+working set (one 33 MB accumulation buffer) fits in L2, so L2 is flushed by
+writing a 256 MB buffer between timed steps.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun (N > 1) every rank renders the full frame (replicas; weak
@@ -98,7 +101,7 @@ def run_reference(args, world, rank):
     b = scenes.mandelbulb_path(W, H, SPP, BOUNCES)
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    stride, rows = 16, (H // 2 - 8, H // 2 + 8)
+    stride, rows = 4, (H // 2 - 32, H // 2 + 32)
     paths = ((rows[1] - rows[0]) * ((W + stride - 1) // stride)) * SPP
     for _ in range(max(args.warmup, 0) and 1):
         oracle.render(b.cfg, b.ext, rows=(rows[0], rows[0] + 1), x_stride=stride)
@@ -121,6 +124,24 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# Algorithmic work of one power-8 Mandelbulb DE evaluation (8 iterations),
+# counted on the reference's trigonometric form (src/mandelbulber/orbit.rs:
+# 529-585): 25 FP32 ops + 7 SFU ops per iteration.
+DE_FP32_OPS, DE_SFU_OPS = 200, 56
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12       # nominal: no measured FP32 peak on this machine
+SFU_PEAK_TOPS = 152 * 16 * 2.070e9 / 1e12
+MLP_FLOP = 2 * (99 * 64 + 3 * 64 * 64 + 64)              # one network row (37.3 kFLOP)
+
+
+def surrogate_config():
+    """Training recipe of the learned skip: 16M points labelled by the exact DE (50% uniform in the
+    box, 50% within 0.05 of the surface), asymmetric loss with 10x weight on overestimates."""
+    from fractalpathtracer_gb300 import native_ext as nx, scenes
+    lo, hi = scenes.SURROGATE_BOXES["mandelbulb"]
+    return nx.mlp_config(lo, hi, points=1 << 24, near_fraction=0.5, near_band=0.05, batch=16384, steps=4000,
+                         lr=2e-3, overestimate_weight=10.0, seed=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -128,19 +149,27 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--only", default="", choices=["", "plain", "box", "skip"],
+                    help="render only this march (profiling runs: no training unless skip, no JSON contract line)")
+    ap.add_argument("--res", default=f"{W}x{H}", help="--only runs: image size WxH")
+    ap.add_argument("--spp", type=int, default=SPP, help="--only runs: samples per pixel")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
+    if args.only:
+        run_only(args)
+        return
 
+    import ctypes
     import numpy as np
     import torch
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    from fractalpathtracer_gb300 import build, native, scenes
+    from fractalpathtracer_gb300 import build, native, native_ext as nx, scenes
     build.build()
     native.lib()
     b = scenes.mandelbulb_path(W, H, SPP, BOUNCES)
@@ -153,70 +182,149 @@ def main():
             torch.distributed.barrier()
             torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        native.cuda_render(cfg, ext, linear=False)
-    # device-timed steps
-    barrier()
-    dev_ms = []
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
+    def series(e, steps, clocks=None):
+        """Device-timed renders (library CUDA events) with L2 flushed before each; per-kernel spans recorded."""
+        out = {"ms": [], "march_ms": 0.0, "march_launches": 0, "march_evals": 0, "skip_ms": 0.0, "shade_ms": 0.0,
+               "launches": 0}
+        for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
-            _, _, ms = native.cuda_render(cfg, ext, linear=False)
-            dev_ms.append(ms)
-    barrier()
-    # end-to-end steps through the C ABI (config upload + linear and RGBA readback)
-    e2e_s = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        native.cuda_render(cfg, ext, linear=True)
-        e2e_s.append(time.perf_counter() - t)
-    barrier()
-    total_ms = sum(dev_ms)
-    e2e_total = sum(e2e_s)
-    if world > 1:
-        t = torch.tensor([total_ms, e2e_total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms, e2e_total = t.tolist()
+            _, _, ms, prof = native.cuda_render(cfg, e, linear=False, profile=True)
+            rs = nx.render_stats()
+            out["ms"].append(ms)
+            out["march_ms"] += rs["march_ms"]
+            out["march_launches"] += rs["march_launches"]
+            out["march_evals"] += rs["march_evals"]
+            out["skip_ms"] += rs["skip_ms"]
+            out["shade_ms"] += rs["shade_ms"]
+            out["launches"] += rs["kernel_launches"]
+        return out
+
+    def e2e_series(e, steps):
+        times = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            native.cuda_render(cfg, e, linear=True)
+            times.append(time.perf_counter() - t)
+        return times
+
+    def reduce_max(vals):
+        if world > 1:
+            t = torch.tensor(vals, device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return t.tolist()
+        return vals
+
     paths = W * H * SPP
-    value = paths * args.steps * world / (total_ms / 1e3) / 1e6
-    e2e = paths * args.steps * world / e2e_total / 1e6
-    # one profiled render for the roofline's algorithmic work count
-    _, _, prof_ms, prof = native.cuda_render(cfg, ext, linear=False, profile=True)
-    evals = prof.distance_evals + prof.normal_evals
-    flop_per_eval = 8 * 53 + 40    # algebraic power-8 step (53 FP32 ops / iteration) + finalize and march bookkeeping
-    achieved_tflops = evals * flop_per_eval / (statistics.median(dev_ms) / 1e3) / 1e12
-    fp32_peak = 152 * 128 * 2 * 2.070e9 / 1e12
+    # ---- plain march
+    for _ in range(args.warmup):
+        native.cuda_render(cfg, ext, linear=False)
+    barrier()
+    plain = series(ext, args.steps)
+    barrier()
+    plain_e2e = e2e_series(ext, args.steps)
+    barrier()
+    # ---- learned skip: train once (outside the timed region), then render
+    model, train = nx.mlp_create(cfg, ext, surrogate_config())
+    skip_ext = ffi_copy(ext)
+    skip_ext.surrogate = 1
+    skip_ext.surrogate_model = model
+    for _ in range(args.warmup):
+        native.cuda_render(cfg, skip_ext, linear=False)
+    barrier()
+    with ClockSampler(local) as clocks:
+        skip = series(skip_ext, args.steps)
+    barrier()
+    skip_stats = nx.skip_stats()
+    skip_e2e = e2e_series(skip_ext, args.steps)
+    barrier()
+    # ---- the same march without the network (the model's box only)
+    box_ext = ffi_copy(skip_ext)
+    box_ext.surrogate = 2
+    for _ in range(args.warmup):
+        native.cuda_render(cfg, box_ext, linear=False)
+    barrier()
+    box = series(box_ext, args.steps)
+    barrier()
+    p_ms, p_e2e, s_ms, s_e2e, b_ms = reduce_max([sum(plain["ms"]), sum(plain_e2e), sum(skip["ms"]), sum(skip_e2e),
+                                                 sum(box["ms"])])
+    plain_value = paths * args.steps * world / (p_ms / 1e3) / 1e6
+    plain_e2e_v = paths * args.steps * world / p_e2e / 1e6
+    value = paths * args.steps * world / (s_ms / 1e3) / 1e6
+    e2e = paths * args.steps * world / s_e2e / 1e6
+    # ---- equal hit distance: primary rays of the same camera, plain vs skip march
+    hp, _ = native.trace_primary(cfg, ext)
+    hs, _ = native.trace_primary(cfg, skip_ext)
+    both = (hp["hit"] > 0) & (hs["hit"] > 0)
+    dt = np.abs(hp["distance"][both].astype(np.float64) - hs["distance"][both]) / (1.0 + hp["distance"][both])
+    hit_agree = float(((hp["hit"] > 0) == (hs["hit"] > 0)).mean())
+    nx.mlp_destroy(model)
+    # ---- roofline of the dominant kernel (the march kernel), timed live over the timed region
+    dom = "march_kernel" if skip["march_ms"] >= skip["skip_ms"] else "skip_march_kernel"
+    march_launch_ms = skip["march_ms"] / max(skip["march_launches"], 1)
+    evals_per_launch = skip["march_evals"] / max(skip["march_launches"], 1)
+    achieved = evals_per_launch * DE_FP32_OPS / (march_launch_ms / 1e3) / 1e12
+    plain_march_tflops = plain["march_evals"] * DE_FP32_OPS / (plain["march_ms"] / 1e3) / 1e12
     clk = clocks.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": s_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"power-8 Mandelbulb path tracing {W}x{H} {SPP}spp {BOUNCES} bounces, RR after 2",
-                   "march": "plain", "l2": "flushed (256 MB write) between steps", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 30448 + 176,
+                   "march": "surrogate-skip (value) vs plain", "l2": "flushed (256 MB write) between steps",
+                   "parallelism": f"replicas x{world}",
+                   "surrogate": "3->99 Fourier->4x64 SiLU->1 bf16, 16M points (50% near-surface), 4000 Adam steps"},
+        "plain": {"value": plain_value, "e2e": plain_e2e_v, "ms_per_step": p_ms / args.steps,
+                  "de_evals_per_s": plain["march_evals"] / (sum(plain["ms"]) / 1e3)},
+        "skip_over_plain": value / plain_value,
+        "box_only": {"value": paths * args.steps * world / (b_ms / 1e3) / 1e6, "ms_per_step": b_ms / args.steps,
+                     "march_evals": box["march_evals"] // args.steps,
+                     "note": "surrogate's box clip without the network (FPT_CUDA_SURROGATE_BOX)"},
+        "hit_equality": {"primary_rays": W * H, "hit_agreement": hit_agree,
+                         "p99_rel_dist_delta": float(np.percentile(dt, 99)) if dt.size else None,
+                         "max_rel_dist_delta": float(dt.max()) if dt.size else None},
+        "skip": {"exact_evals_in_skip": skip_stats["exact_evals"],
+                 "march_evals": skip["march_evals"] // args.steps, "plain_march_evals": plain["march_evals"] // args.steps,
+                 "network_rows": skip_stats["rows"], "accepted": skip_stats["accepted"],
+                 "rejected": skip_stats["rejected"], "escaped": skip_stats["escaped"],
+                 "skip_ms": skip["skip_ms"] / args.steps, "march_ms": skip["march_ms"] / args.steps,
+                 "shade_ms": skip["shade_ms"] / args.steps, "train_ms": train["train_ms"], "data_ms": train["data_ms"],
+                 "loss_first": train["loss_first"], "loss_last": train["loss_last"]},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": ctypes.sizeof(cfg) + ctypes.sizeof(ext),
                 "d2h_bytes_per_step": W * H * 16 + W * H * 4},
-        "gpu_launches": 2 * args.steps,
-        "de_evals_per_s": evals / (statistics.median(dev_ms) / 1e3),
-        "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved_tflops / fp32_peak, "traffic": None,
+        "gpu_launches": skip["launches"],
+        "de_evals_per_s": (skip["march_evals"] + skip_stats["exact_evals"] * args.steps) / (sum(skip["ms"]) / 1e3),
+        "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "frac": achieved / FP32_PEAK_TFLOPS, "traffic": None,
+                     "sfu_frac": achieved / DE_FP32_OPS * DE_SFU_OPS / SFU_PEAK_TOPS,
+                     "plain_march_frac": plain_march_tflops / FP32_PEAK_TFLOPS,
+                     "work": f"{DE_FP32_OPS} FP32 + {DE_SFU_OPS} SFU ops per DE evaluation x march-kernel evaluations",
                      "peak_source": "nominal 152 SM x 128 FP32 lanes x 2 x 2070 MHz (no measured FP32 peak)"},
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
     }
+    if skip["skip_ms"] > 0:
+        rows = skip_stats["forwards"] * 32   # per render (the statistics of the last render)
+        tflops = rows * MLP_FLOP / (skip["skip_ms"] / args.steps / 1e3) / 1e12
+        peaks = measured_peaks()
+        line["roofline_skip_kernel"] = {"bound": "tensor", "achieved": tflops,
+                                        "peak": peaks.get("bf16_tflops", 1900.0), "unit": "TFLOP/s",
+                                        "frac": tflops / peaks.get("bf16_tflops", 1900.0),
+                                        "peak_source": "MEASURED_PEAKS.json bf16 burst" if peaks else "fallback"}
     if rank == 0 and args.cpu_baseline:
         try:
             import oracle
             cores = os.cpu_count() or 1
             oracle.set_threads(cores)
-            stride, rows = 32, (H // 2 - 4, H // 2 + 4)
+            stride, rows = 2, (H // 2 - 135, H // 2 + 135)
             t = time.perf_counter()
             oracle.render(cfg, ext, rows=rows, x_stride=stride)
-            dt = time.perf_counter() - t
+            dt_cpu = time.perf_counter() - t
             n = (rows[1] - rows[0]) * ((W + stride - 1) // stride) * SPP
-            line["cpu_baseline"] = {"value": n / dt / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
-                                    "sample": f"rows {rows[0]}-{rows[1]}, every {stride}th column, {SPP} spp"}
+            line["cpu_baseline"] = {"value": n / dt_cpu / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+                                    "sample": f"plain march, central rows {rows[0]}-{rows[1]}, every {stride}nd column, "
+                                              f"{SPP} spp ({n} paths, {dt_cpu:.1f} s)"}
         except Exception as exc:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                     "sample": f"failed: {exc}"}
@@ -224,6 +332,35 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_only(args):
+    """One march variant at the bench workload, for profiler launch lists (small surrogate for skip/box)."""
+    from fractalpathtracer_gb300 import build, native, native_ext as nx, scenes
+    build.build()
+    w, h = (int(v) for v in args.res.lower().split("x"))
+    b = scenes.mandelbulb_path(w, h, args.spp, BOUNCES)
+    cfg, ext = b.cfg, b.ext
+    model = None
+    if args.only != "plain":
+        lo, hi = scenes.SURROGATE_BOXES["mandelbulb"]
+        model, _ = nx.mlp_create(cfg, ext, nx.mlp_config(lo, hi, points=1 << 20, steps=400, batch=8192, seed=1))
+        ext = ffi_copy(ext)
+        ext.surrogate = 1 if args.only == "skip" else 2
+        ext.surrogate_model = model
+    for _ in range(args.warmup):
+        native.cuda_render(cfg, ext, linear=False)
+    ms = [native.cuda_render(cfg, ext, linear=False)[2] for _ in range(args.steps)]
+    print(json.dumps({"only": args.only, "ms": ms, "stats": nx.render_stats()}), flush=True)
+    if model is not None:
+        nx.mlp_destroy(model)
+
+
+def ffi_copy(ext):
+    import ctypes
+    out = type(ext)()
+    ctypes.memmove(ctypes.byref(out), ctypes.byref(ext), ctypes.sizeof(ext))
+    return out
 
 
 if __name__ == "__main__":

@@ -375,6 +375,19 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
             return 1;
         pl.skip = &skip;
     }
+    KernelTimer timer;
+    uint64_t launches = 0;
+    pl.launches = &launches;
+    if (want_profile) {
+        if (!c.timer_events) {
+            c.timer_capacity = 1024;
+            c.timer_events = new cudaEvent_t[c.timer_capacity];
+            for (int i = 0; i < c.timer_capacity; ++i) cudaEventCreate(&c.timer_events[i]);
+        }
+        timer.events = c.timer_events;
+        timer.capacity = c.timer_capacity;
+        pl.timer = &timer;
+    }
     for (uint32_t start = 0; start < spp; start += step) {
         uint32_t end = std::min(spp, start + step);
         for (uint32_t a = start; a < end; a += sub_cap) {
@@ -384,11 +397,28 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         }
     }
     if (!check(launch_present(c.scene, S.width, S.height, c.accum, c.rgba, c.stream), "present launch", error, error_len)) return 1;
+    ++launches;
     cudaEventRecord(c.ev1, c.stream);
     if (!check(cudaStreamSynchronize(c.stream), "CUDA render", error, error_len)) return 1;
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     if (elapsed_ms) *elapsed_ms = double(ms);
+    {
+        FptCudaRenderStats &rs = c.last_render;
+        std::memset(&rs, 0, sizeof(rs));
+        rs.kernel_launches = launches + (hydrated.focus_distance <= 0.0f ? 1u : 0u);
+        rs.total_ms = ms;
+        double cat_ms[KC_COUNT] = {0.0, 0.0, 0.0};
+        uint64_t cat_n[KC_COUNT] = {0, 0, 0};
+        for (int i = 0; i < timer.n; ++i) {
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, timer.events[2 * i], timer.events[2 * i + 1]);
+            cat_ms[timer.cat[i]] += t;
+            cat_n[timer.cat[i]] += 1;
+        }
+        rs.march_ms = cat_ms[KC_MARCH]; rs.shade_ms = cat_ms[KC_SHADE]; rs.skip_ms = cat_ms[KC_SKIP];
+        rs.march_launches = cat_n[KC_MARCH]; rs.shade_launches = cat_n[KC_SHADE]; rs.skip_launches = cat_n[KC_SKIP];
+    }
     std::vector<uint8_t> host_rgba;
     uint8_t *rgba = rgba_output;
     if (!rgba) { host_rgba.resize(pixels * 4); rgba = host_rgba.data(); }
@@ -407,7 +437,9 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         if (!check(cudaMemcpy(v, c.profile, sizeof(v), cudaMemcpyDeviceToHost), "profile readback", error, error_len)) return 1;
         profile_out->primary_steps = v[0]; profile_out->secondary_steps = v[1]; profile_out->shadow_steps = v[2];
         profile_out->normal_evals = v[3]; profile_out->bounces = v[4]; profile_out->pixels = v[5];
-        profile_out->distance_evals = v[6]; profile_out->material_evals = v[7];
+        profile_out->distance_evals = v[0] + v[1] + v[2]; profile_out->material_evals = v[7];
+        c.last_render.march_evals = v[0] + v[1] + v[2];
+        c.last_render.shade_evals = v[3] + v[7];
         profile_out->distance_evals_by_phase[0] = v[0];
         profile_out->distance_evals_by_phase[1] = v[1];
         profile_out->distance_evals_by_phase[2] = v[2];
@@ -618,6 +650,13 @@ int fpt_metal_preview(const char *metallib_path, const char *stitch_metallib_pat
     (void)config; (void)scene_configs; (void)scene_config_count; (void)scene_config_index;
     set_error(error, error_len, "unsupported: interactive preview needs a window system, which a headless CUDA node lacks");
     return 1;
+}
+
+int fpt_cuda_render_stats(struct FptCudaRenderStats *stats) {
+    if (!stats) return 1;
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    *stats = ctx().last_render;
+    return 0;
 }
 
 }  // extern "C"

@@ -30,6 +30,8 @@ struct Context {
     float *grads = nullptr; size_t cap_grads = 0;
     unsigned long long *skip_stats = nullptr; size_t cap_skip_stats = 0;
     unsigned long long last_skip[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // counters of the last skip-march call
+    cudaEvent_t *timer_events = nullptr; int timer_capacity = 0;   // per-kernel timing pool (profile renders)
+    FptCudaRenderStats last_render = {};
     // launch tuning (set by the autotuner entry point; 0 = defaults)
     uint32_t wave_paths = 0;   // paths per wave; 0 = min(all paths, 16M)
     int march_blocks = 0;

@@ -9,6 +9,28 @@ namespace fpt {
 
 struct SkipArgs;   // skip.cuh
 
+// CUDA-event spans around kernel launches (per-kernel device time of a
+// render).  Events come from a pool created by the caller; spans past the
+// pool's capacity are not timed.
+enum KernelCategory : int { KC_MARCH = 0, KC_SHADE = 1, KC_SKIP = 2, KC_COUNT = 3 };
+struct KernelTimer {
+    cudaEvent_t *events = nullptr;
+    int capacity = 0;   // events in the pool
+    int used = 0;
+    int cat[512];
+    int n = 0;          // completed spans
+    bool begin(int c, cudaStream_t st) {
+        if (!events || used + 2 > capacity || n >= 512) return false;
+        cat[n] = c;
+        cudaEventRecord(events[used++], st);
+        return true;
+    }
+    void end(cudaStream_t st) {
+        cudaEventRecord(events[used++], st);
+        ++n;
+    }
+};
+
 // Bytes of wave scratch per path: path record (96), two march queues (8),
 // two shadow queues (128), shade queue (4).
 constexpr size_t kWaveBytesPerPath = 96 + 8 + 128 + 4;
@@ -27,6 +49,8 @@ struct PathLaunch {
     int march_blocks;           // persistent march grid, <= 0 = one wave of resident blocks
     unsigned long long *profile;  // 8 device counters or null
     const SkipArgs *skip;       // surrogate-skip pass before each march pass, or null
+    KernelTimer *timer;         // per-kernel event spans, or null
+    uint64_t *launches;         // host counter of kernel launches, or null
 };
 
 cudaError_t launch_pathtrace(const PathLaunch &pl, cudaStream_t stream);

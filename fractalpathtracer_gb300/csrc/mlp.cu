@@ -430,9 +430,10 @@ bool surrogate_args(uint64_t model, const DeviceScene &S, unsigned long long *st
     }
     A.M = hm->view();
     for (int k = 0; k < 3; ++k) { A.lo[k] = hm->lo[k]; A.hi[k] = hm->hi[k]; }
-    A.margin = S.surrogate_margin > 0.0f ? S.surrogate_margin : 0.01f;
+    A.margin = S.surrogate_margin > 0.0f ? S.surrogate_margin : 0.1f;
     A.safety = S.surrogate_safety > 0.0f ? S.surrogate_safety : 0.9f;
     A.max_iters = 64;
+    A.use_network = S.surrogate == FPT_CUDA_SURROGATE_SKIP ? 1u : 0u;
     A.stats = stats;
     return true;
 }

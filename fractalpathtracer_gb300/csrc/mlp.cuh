@@ -4,10 +4,12 @@
 // Network: 3-D point -> 99 Fourier features (the normalised point and
 // sin/cos of pi * f_k * u_i for 16 log-spaced frequencies f_k = 2^(6k/15))
 // -> 4 hidden layers of 64 SiLU units -> 1 output (distance / label_scale).
-// BF16 weights and activations, FP32 accumulation.
+// BF16 weights and activations, FP32 accumulation.  Training evaluates SiLU
+// with an f32 tanh; inference takes the sigmoid from a packed f16x2 tanh.
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -219,28 +221,129 @@ __device__ __forceinline__ void dense_layer(const __nv_bfloat16 *hin, int sin, c
     __syncwarp();
 }
 
-// Per-warp scratch of the forward pass.  dense_layer reads all of its input
-// before it writes its output, so the layers run in place: one buffer holds
-// the features, then each hidden layer's activations (stride kStrideH).
+// Per-warp scratch of the forward pass: the 32 feature rows (layer 0 reads
+// them through ldmatrix; the hidden layers stay in registers).
 struct WarpForward {
     __nv_bfloat16 x[32 * kStrideIn];
 };
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+// SiLU of two values for inference: sigmoid from one packed f16x2 tanh
+// (half the MUFU work of two f32 tanh), product and rounding in f32.
+__device__ __forceinline__ uint32_t silu2_bf16(float z0, float z1) {
+    const __half2 hz = __floats2half2_rn(0.5f * z0, 0.5f * z1);
+    uint32_t t, s;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const uint32_t *>(&hz)));
+    asm("fma.rn.f16x2 %0, %1, %2, %2;" : "=r"(s) : "r"(t), "r"(0x38003800u));   // 0.5 t + 0.5
+    const float2 sf = __half22float2(*reinterpret_cast<const __half2 *>(&s));
+    return pack_bf16(z0 * sf.x, z1 * sf.y);
+}
+
+// SiLU epilogue that turns the accumulators of a 32 x 64 layer output (two
+// m16 tiles x eight n8 tiles) into the A fragments of the next layer's
+// m16n8k16 products: n-tiles 2kb and 2kb+1 hold exactly the (row, k) pairs of
+// k-block kb (row g: c0 c1, row g+8: c2 c3), so no shared memory is needed.
+__device__ __forceinline__ void silu_to_fragments(const float acc[2][8][4], const float *bias, uint32_t a[2][4][4], int lane) {
+    const int t = lane & 3;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+            const int col = n * 8 + t * 2;
+            const float b0 = bias[col], b1 = bias[col + 1];
+            a[m][n >> 1][(n & 1) * 2 + 0] = silu2_bf16(acc[m][n][0] + b0, acc[m][n][1] + b1);
+            a[m][n >> 1][(n & 1) * 2 + 1] = silu2_bf16(acc[m][n][2] + b0, acc[m][n][3] + b1);
+        }
+}
+
+// acc = A (registers, 32 x 64) x W^T, W [64 x 64] in shared memory.
+__device__ __forceinline__ void hidden_product(const uint32_t a[2][4][4], const __nv_bfloat16 *w, float acc[2][8][4], int lane) {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < 8; ++n)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.0f;
+#pragma unroll
+    for (int kb = 0; kb < 4; ++kb)
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+            uint32_t b[2];
+            load_b_nk(b, w, kStrideH, n * 8, kb * 16, lane);
+            mma16816(acc[0][n], a[0][kb], b);
+            mma16816(acc[1][n], a[1][kb], b);
+        }
+}
 
 // Forward pass of 32 points (one per lane, normalised coordinates u); returns
 // this lane's output (in label units).  All lanes of the warp must call it.
 __device__ __forceinline__ float forward32(const SmemWeights &sw, WarpForward &wf, const float u[3], int lane) {
     features(u, wf.x + lane * kStrideIn);
     __syncwarp();
-    dense_layer<kInPad>(wf.x, kStrideIn, sw.w0, kStrideIn, sw.b[0], nullptr, 0, wf.x, lane);
-    dense_layer<kHid>(wf.x, kStrideH, sw.w[0], kStrideH, sw.b[1], nullptr, 0, wf.x, lane);
-    dense_layer<kHid>(wf.x, kStrideH, sw.w[1], kStrideH, sw.b[2], nullptr, 0, wf.x, lane);
-    dense_layer<kHid>(wf.x, kStrideH, sw.w[2], kStrideH, sw.b[3], nullptr, 0, wf.x, lane);
-    const __nv_bfloat16 *h4 = wf.x + lane * kStrideH;
-    float out = sw.b4;
-#pragma unroll 8
-    for (int j = 0; j < kHid; ++j) out += __bfloat162float(h4[j]) * sw.w4[j];
-    __syncwarp();
-    return out;
+    float acc[2][8][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < 8; ++n)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.0f;
+#pragma unroll
+    for (int k0 = 0; k0 < kInPad; k0 += 16) {
+        uint32_t a0[4], a1[4];
+        load_a(a0, wf.x, kStrideIn, 0, k0, lane);
+        load_a(a1, wf.x, kStrideIn, 16, k0, lane);
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+            uint32_t b[2];
+            load_b_nk(b, sw.w0, kStrideIn, n * 8, k0, lane);
+            mma16816(acc[0][n], a0, b);
+            mma16816(acc[1][n], a1, b);
+        }
+    }
+    __syncwarp();   // the feature rows may be rewritten by the next call
+    uint32_t a[2][4][4];
+    silu_to_fragments(acc, sw.b[0], a, lane);
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        hidden_product(a, sw.w[l], acc, lane);
+        silu_to_fragments(acc, sw.b[l + 1], a, lane);
+    }
+    hidden_product(a, sw.w[2], acc, lane);
+    // Output layer: per-row dot product of the (bf16-rounded) last activations
+    // with W4, reduced over the quad that holds the row.
+    const int t = lane & 3;
+    float part[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+            const int col = n * 8 + t * 2;
+            const float b0 = sw.b[3][col], b1 = sw.b[3][col + 1], w0 = sw.w4[col], w1 = sw.w4[col + 1];
+            const uint32_t hlo = silu2_bf16(acc[m][n][0] + b0, acc[m][n][1] + b1);
+            const uint32_t hhi = silu2_bf16(acc[m][n][2] + b0, acc[m][n][3] + b1);
+            const float h0 = __uint_as_float(hlo << 16), h1 = __uint_as_float(hlo & 0xffff0000u);
+            const float h2 = __uint_as_float(hhi << 16), h3 = __uint_as_float(hhi & 0xffff0000u);
+            part[m][0] += h0 * w0 + h1 * w1;
+            part[m][1] += h2 * w0 + h3 * w1;
+        }
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            part[m][h] += __shfl_xor_sync(0xffffffffu, part[m][h], 1);
+            part[m][h] += __shfl_xor_sync(0xffffffffu, part[m][h], 2);
+        }
+    // lane L holds row L: m-tile L / 16, row (L % 16) = g + 8 h, held by lane 4 g
+    const int src = (lane & 7) * 4;
+    const float v00 = __shfl_sync(0xffffffffu, part[0][0], src), v01 = __shfl_sync(0xffffffffu, part[0][1], src);
+    const float v10 = __shfl_sync(0xffffffffu, part[1][0], src), v11 = __shfl_sync(0xffffffffu, part[1][1], src);
+    const bool upper = (lane & 8) != 0;
+    const float dot = lane < 16 ? (upper ? v01 : v00) : (upper ? v11 : v10);
+    return sw.b4 + dot;
 }
 
 }  // namespace mlp

@@ -26,6 +26,12 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     W.sample_rgb = pl.sample_rgb;
     W.counters = pl.counters;
     W.profile = pl.profile;
+    W.box_on = pl.skip ? 1u : 0u;
+    for (int k = 0; k < 3; ++k) {
+        W.box_lo[k] = pl.skip ? pl.skip->lo[k] : 0.0f;
+        W.box_hi[k] = pl.skip ? pl.skip->hi[k] : 0.0f;
+    }
+    const bool skip_pass = pl.skip && pl.skip->use_network;
     const uint32_t cap = pl.wave_paths;
     char *base = static_cast<char *>(pl.wave_scratch);
     W.paths = reinterpret_cast<PathRec *>(base);
@@ -43,7 +49,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         march_blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
     int skip_blocks = 0;
-    if (pl.skip) {
+    if (skip_pass) {
         static bool attr = false;
         if (!attr) {
             cudaFuncSetAttribute(skip_march_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(skip_smem_bytes()));
@@ -57,25 +63,40 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_per_sm, shade_kernel<KIND>, 128, 0);
     const int shade_blocks = sms * (shade_per_sm > 0 ? shade_per_sm : 1);
     const uint64_t total = uint64_t(W.pixel_work) * W.sample_count;
+    uint64_t launches = 0;
+    auto timed = [&](int category, auto &&launch) {
+        const bool t = pl.timer && pl.timer->begin(category, stream);
+        launch();
+        if (t) pl.timer->end(stream);
+        ++launches;
+    };
     cudaError_t e = cudaSuccess;
     for (uint64_t wb = 0; wb < total; wb += cap) {
         W.wave_base = uint32_t(wb);
         W.n_paths = uint32_t(std::min<uint64_t>(cap, total - wb));
         if ((e = cudaMemsetAsync(W.counters, 0, C_COUNT * sizeof(uint32_t), stream)) != cudaSuccess) return e;
         camera_kernel<<<std::min<uint32_t>((W.n_paths + 255u) / 256u, uint32_t(sms) * 16u), 256, 0, stream>>>(W);
+        ++launches;
         for (uint32_t b = 0; b <= pl.bounces; ++b) {
             const int cur = int(b & 1u);
             reset_counters_kernel<<<1, 32, 0, stream>>>(W.counters, cur ^ 1);
-            if (pl.skip) skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, cur, *pl.skip);
-            march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
-            if (b < pl.bounces) shade_kernel<KIND><<<shade_blocks, 128, 0, stream>>>(W, cur);
+            ++launches;
+            if (skip_pass)
+                timed(KC_SKIP, [&] {
+                    skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, cur, *pl.skip);
+                });
+            timed(KC_MARCH, [&] { march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur); });
+            if (b < pl.bounces) timed(KC_SHADE, [&] { shade_kernel<KIND><<<shade_blocks, 128, 0, stream>>>(W, cur); });
         }
         finalize_kernel<<<(W.n_paths + 255u) / 256u, 256, 0, stream>>>(W);
+        ++launches;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     const uint32_t pixels = pl.width * pl.height;
     reduce_samples_kernel<<<(pixels + 255u) / 256u, 256, 0, stream>>>(pl.sample_rgb, pl.accum, pixels, pl.sample_begin,
                                                                        W.sample_count);
+    ++launches;
+    if (pl.launches) *pl.launches += launches;
     return cudaGetLastError();
 }
 

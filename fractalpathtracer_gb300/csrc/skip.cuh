@@ -1,12 +1,15 @@
 // skip.cuh -- surrogate-skip march: learned step proposals, certified by the exact DE.
 //
 // A ray at p with exact distance d_p = DE(p) asks the network for the
-// distance m at the look-ahead point p + 2 d_p dir and proposes the step
+// distance m at the look-ahead point p + lambda d_p dir and proposes the step
 // s = d_p + safety * m.  The exact DE at q = p + s dir decides:
 //   s <= d_p + DE(q)   the balls of radius d_p around p and DE(q) around q
 //                      hold no surface and overlap, so [p, q] is free:
 //                      the ray moves to q (one exact evaluation for s)
 //   otherwise          plain step 0.99 d_p (the reference march rule)
+// lambda adapts per ray: 1.5 s / d_p after an accepted step (rays leaving a
+// surface look further ahead each step), 2 after a refusal.  The exact march
+// takes over where the distance is under the hand-over margin.
 // Every step is certified by the exact DE, so the surrogate only changes how
 // far a ray gets per evaluation, never what it hits.  When d_p falls below
 // the hand-over margin the exact march (march_update) finishes the ray.
@@ -30,13 +33,14 @@ struct SkipArgs {
     float margin;                // hand over to the exact march below this distance
     float safety;                // scale of the predicted distance in a proposal
     uint32_t max_iters;          // skip iterations per ray before hand-over
+    uint32_t use_network;        // 0: box clip only (the march kernel applies it; no skip pass)
     unsigned long long *stats;   // kSkipStats counters or null
 };
 
 enum SkipStat : int { SK_ROWS = 0, SK_FORWARDS = 1, SK_EXACT = 2, SK_ACCEPT = 3, SK_REJECT = 4, SK_ESCAPE = 5, SK_HANDOVER = 6,
                       SK_DIST = 7, kSkipStats = 8 };
 
-constexpr int kSkipWarps = 8;
+constexpr int kSkipWarps = 4;
 inline size_t skip_smem_bytes() { return ((sizeof(mlp::SmemWeights) + 127) & ~size_t(127)) + kSkipWarps * sizeof(mlp::WarpForward); }
 
 // Forward slab test: [tn, tf] of the ray inside the box, tn >= 0.
@@ -65,6 +69,7 @@ struct SkipLane {
     float t;              // advance along dir from origin
     float t_exit;         // box exit (advance)
     float d;              // exact distance at origin + t dir (SP_PROPOSE)
+    float lam;            // look-ahead in units of d
     int phase;
     uint32_t iters;
 };
@@ -77,6 +82,7 @@ __device__ __forceinline__ bool skip_begin(SkipLane &L, const SkipArgs &A, float
     L.t = 0.0f;
     L.iters = 0;
     L.d = 0.0f;
+    L.lam = 2.0f;
     float tn, tf;
     if (!box_span(A, origin, dir, tn, tf)) { L.phase = SP_IDLE; return false; }
     L.t = tn;
@@ -94,11 +100,11 @@ __device__ __forceinline__ int skip_step(SkipLane &L, const DeviceScene &S, cons
                                          mlp::WarpForward &wf, int lane, uint32_t &c_rows, uint32_t &c_fwd, uint32_t &c_exact,
                                          uint32_t &c_acc, uint32_t &c_rej) {
     const unsigned FULL = 0xffffffffu;
-    const bool propose = L.phase == SP_PROPOSE;
+    const bool propose = A.use_network && L.phase == SP_PROPOSE;
     float3 p = L.origin + L.dir * L.t;
     float m = 0.0f;
     if (__any_sync(FULL, propose)) {
-        float3 q0 = propose ? p + L.dir * (2.0f * L.d) : p;
+        float3 q0 = propose ? p + L.dir * (L.lam * L.d) : p;
         float u[3] = {(q0.x - A.M.center[0]) * A.M.inv_half[0], (q0.y - A.M.center[1]) * A.M.inv_half[1],
                       (q0.z - A.M.center[2]) * A.M.inv_half[2]};
 #pragma unroll
@@ -118,16 +124,20 @@ __device__ __forceinline__ int skip_step(SkipLane &L, const DeviceScene &S, cons
             L.t += 0.99f * L.d;
             L.phase = SP_EXACT;
         }
+    } else if (L.phase == SP_PROPOSE) {   // box-only mode: plain steps
+        L.t += 0.99f * L.d;
     }
     const float3 e_pt = L.origin + L.dir * (cand ? L.t + s : L.t);
     const float de = scene_eval<KIND>(S, e_pt, EV_MAP).d;
     ++c_exact;
     if (cand) {
         if (s <= L.d + de && isfinite(de)) {
+            L.lam = fminf(fmaxf(1.5f * s / L.d, 2.0f), 32.0f);
             L.t += s;
             L.d = de;
             ++c_acc;
         } else {
+            L.lam = 2.0f;
             L.t += 0.99f * L.d;
             L.phase = SP_EXACT;
             ++c_rej;
@@ -137,6 +147,9 @@ __device__ __forceinline__ int skip_step(SkipLane &L, const DeviceScene &S, cons
         L.phase = SP_PROPOSE;
     }
     if (L.t >= L.t_exit) return SO_ESCAPE;
+    // Hand over near a surface.  (Keeping rays that leave a surface in the
+    // skip pass until their distance stops growing cost more exact
+    // evaluations than it saved on the power-8 Mandelbulb at 1080p.)
     if (L.phase == SP_PROPOSE && (!isfinite(L.d) || fabsf(L.d) < A.margin)) return SO_HANDOVER;
     if (++L.iters >= A.max_iters) return SO_HANDOVER;
     return SO_CONTINUE;
@@ -161,7 +174,7 @@ __device__ __forceinline__ void skip_flush_stats(const SkipArgs &A, int lane, ui
 // normal.w; escapes set dir.w = 1 (unoccluded).  Jobs are taken with
 // per-lane regeneration from counter C_SKIP.
 template <int KIND>
-__global__ void __launch_bounds__(32 * kSkipWarps, 2) skip_march_kernel(WaveParams W, int cur, SkipArgs A) {
+__global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WaveParams W, int cur, SkipArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::SmemWeights &sw = *reinterpret_cast<mlp::SmemWeights *>(smem_raw);
     mlp::WarpForward *wf_all =
@@ -181,8 +194,6 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 2) skip_march_kernel(WavePara
     uint32_t job = 0;
     bool shadow = false;
     uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
-    uint32_t c_primary = 0, c_secondary = 0, c_shadow = 0;
-    uint32_t bounce = 0;
     while (true) {
         // Refill idle lanes (one atomic per warp); rays that miss the box are
         // resolved at once and the lane draws again.
@@ -205,7 +216,6 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 2) skip_march_kernel(WavePara
                         const PathRec &R = W.paths[job];
                         o = mk3(R.pos.x, R.pos.y, R.pos.z);
                         d = mk3(R.dir.x, R.dir.y, R.dir.z);
-                        bounce = fbits(R.color.w) & 0xffu;
                     } else {
                         job = idx - n_path;
                         const ShadowJob &J = W.q_shadow[cur][job];
@@ -225,41 +235,38 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 2) skip_march_kernel(WavePara
             continue;
         }
         const int out = skip_step<KIND>(L, S, A, sw, wf, lane, c_rows, c_fwd, c_exact, c_acc, c_rej);
-        if (L.phase != SP_IDLE) {
-            if (shadow) ++c_shadow; else if (bounce == 0u) ++c_primary; else ++c_secondary;
-        }
         if (L.phase != SP_IDLE && out != SO_CONTINUE) {
             if (out == SO_ESCAPE) ++c_esc; else ++c_hand;
+            const bool known = out == SO_HANDOVER && L.phase == SP_PROPOSE;   // L.d is the exact distance here
             if (!shadow) {
                 PathRec &R = W.paths[job];
                 float3 p = L.origin + L.dir * L.t;
                 R.pos = make_float4(p.x, p.y, p.z, R.pos.w);
                 if (out == SO_ESCAPE) R.color.w = bitsf(fbits(R.color.w) | PF_ESCAPED);
+                if (known) {
+                    R.grad.w = L.d;
+                    R.color.w = bitsf(fbits(R.color.w) | PF_KNOWN_D);
+                }
             } else {
                 ShadowJob &J = W.q_shadow[cur][job];
                 J.normal.w = L.t;
                 if (out == SO_ESCAPE) J.dir.w = 1.0f;
+                if (known) {
+                    J.contrib.w = L.d;
+                    J.dir.w = 2.0f;
+                }
             }
             L.phase = SP_IDLE;
         }
     }
     skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
-    if (W.profile) {
-        uint32_t v[3] = {c_primary, c_secondary, c_shadow};
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            uint32_t s = v[k];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
-            if (lane == 0 && s) atomicAdd(W.profile + k, (unsigned long long)s);
-        }
-    }
 }
 
 // Primary rays with the surrogate skip in front of the exact march (the
 // counterpart of trace_primary_kernel): per pixel distance, normal, exact
 // evaluations (skip + march) and hit flag.
 template <int KIND>
-__global__ void __launch_bounds__(32 * kSkipWarps, 2) skip_primary_kernel(const DeviceScene *scene, SkipArgs A,
+__global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_primary_kernel(const DeviceScene *scene, SkipArgs A,
                                                                           FptCudaPrimaryHit *hits) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::SmemWeights &sw = *reinterpret_cast<mlp::SmemWeights *>(smem_raw);

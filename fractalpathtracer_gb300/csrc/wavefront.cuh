@@ -28,8 +28,12 @@
 namespace fpt {
 
 // PF_ESCAPED: the surrogate-skip pass found the ray leaving the geometry's
-// box; the march classifies it as a miss without evaluating.
-enum PathFlags : uint32_t { PF_DONE = 1u << 8, PF_INVISIBLE = 1u << 9, PF_VALID = 1u << 10, PF_ESCAPED = 1u << 11 };
+// box; the march classifies it as a miss without evaluating.  PF_KNOWN_D:
+// the skip pass handed the ray over with the exact distance at its position
+// in grad.w, so the march does not evaluate it again.
+enum PathFlags : uint32_t {
+    PF_DONE = 1u << 8, PF_INVISIBLE = 1u << 9, PF_VALID = 1u << 10, PF_ESCAPED = 1u << 11, PF_KNOWN_D = 1u << 12
+};
 
 struct alignas(16) PathRec {
     float4 pos;     // xyz march origin or hit point, w side
@@ -37,13 +41,14 @@ struct alignas(16) PathRec {
     float4 color;   // xyz throughput, w state bits (bounce | flags)
     float4 light;   // xyz emission + environment light, w slot bits
     float4 shadow;  // xyz sun light from shadow rays
-    float4 grad;    // xyz background gradient colour of the camera ray
+    float4 grad;    // xyz background gradient colour of the camera ray, w exact distance (PF_KNOWN_D)
 };
 
 struct alignas(16) ShadowJob {
     float4 origin;  // xyz hit point, w path index bits
     float4 normal;  // xyz normal the ray leaves along (offset 0.001), w advance made by the skip pass
-    float4 dir;     // xyz light direction, w 1 when the skip pass found the ray leaving the geometry's box
+    float4 dir;     // xyz light direction, w 1 when the skip pass found the ray leaving the geometry's box,
+                    // 2 when it handed the ray over with the exact distance at its start in contrib.w
     float4 contrib; // xyz light added when the ray escapes
 };
 
@@ -64,7 +69,30 @@ struct WaveParams {
     uint32_t tiles_x;
     uint32_t sample_begin, sample_count;
     unsigned long long *profile;   // 8 counters or null
+    // Box holding all geometry (surrogate modes): a march starts where its
+    // ray enters the box and ends as a miss where it leaves it.
+    uint32_t box_on;
+    float box_lo[3], box_hi[3];
 };
+
+// Forward slab test against the wave's box: [tn, tf] with tn >= 0.
+__device__ __forceinline__ bool wave_box_span(const WaveParams &W, float3 p, float3 d, float &tn, float &tf) {
+    tn = 0.0f;
+    tf = 3.0e38f;
+    const float pv[3] = {p.x, p.y, p.z}, dv[3] = {d.x, d.y, d.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (dv[a] != 0.0f) {
+            const float inv = 1.0f / dv[a];
+            const float t0 = (W.box_lo[a] - pv[a]) * inv, t1 = (W.box_hi[a] - pv[a]) * inv;
+            tn = fmaxf(tn, fminf(t0, t1));
+            tf = fminf(tf, fmaxf(t0, t1));
+        } else if (pv[a] < W.box_lo[a] || pv[a] > W.box_hi[a]) {
+            return false;
+        }
+    }
+    return tf >= tn;
+}
 
 __device__ __forceinline__ uint32_t fbits(float v) { return __float_as_uint(v); }
 __device__ __forceinline__ float bitsf(uint32_t v) { return __uint_as_float(v); }
@@ -167,6 +195,10 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
     const float3 cam = mk3(S.cam_pos[0], S.cam_pos[1], S.cam_pos[2]);
     March m;
     MarchJob job;
+    float3 box_origin = mk3(0.0f);   // box mode: ray origin and exit advance of the lane's job
+    float box_exit = 3.0e38f;
+    float known_d = 0.0f;            // exact distance at the march start handed over by the skip pass
+    bool have_d = false;
     bool active = false, pending = false, retired = false;
     uint32_t c_primary = 0, c_secondary = 0, c_shadow = 0, c_paths = 0;
     while (true) {
@@ -185,16 +217,22 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
                     job.shadow = false;
                     const PathRec &R = W.paths[job.path];
                     float4 pos = R.pos, dir = R.dir;
-                    const uint32_t st = fbits(R.color.w);
+                    uint32_t st = fbits(R.color.w);
                     job.bounce = st & 0xffu;
                     int ni = job.bounce == 0u ? int(S.render[1]) : int(S.render[1] / (S.render[5] * 2.0f + 1.0f));
                     float3 o = mk3(pos.x, pos.y, pos.z), dv = mk3(dir.x, dir.y, dir.z);
+                    float tn = 0.0f, tf = 3.0e38f;
+                    if (W.box_on && !(st & PF_ESCAPED) && !wave_box_span(W, o, dv, tn, tf)) st |= PF_ESCAPED;
                     if (st & PF_ESCAPED) {   // a miss: end beyond the far limit
                         active = false;
                         m.steps = 0;
                         m.pos = o + dv * (S.render[4] + len3(o - cam) + 1.0f);
                     } else {
-                        active = march_begin(m, S, o, dv, ni, S.render[3], 0.0002f);
+                        box_origin = o;
+                        box_exit = tf;
+                        active = march_begin(m, S, o + dv * tn, dv, ni, S.render[3], 0.0002f);
+                        have_d = active && (st & PF_KNOWN_D) && tn == 0.0f;
+                        known_d = R.grad.w;
                     }
                     pending = !active;
                 } else {
@@ -205,13 +243,19 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
                     job.contrib = J.contrib;
                     job.rp0 = mk3(o.x, o.y, o.z);
                     float3 dv = mk3(d.x, d.y, d.z);
-                    if (d.w == 1.0f) {   // unoccluded: end beyond the far limit
+                    float3 start = job.rp0 + mk3(nn.x, nn.y, nn.z) * 0.001f + dv * nn.w;
+                    float tn = 0.0f, tf = 3.0e38f;
+                    const bool miss = d.w == 1.0f || (W.box_on && !wave_box_span(W, start, dv, tn, tf));
+                    if (miss) {   // unoccluded: end beyond the far limit
                         active = false;
                         m.steps = 0;
                         m.pos = job.rp0 + dv * (S.render[4] * 1.01f + 1.0f);
                     } else {
-                        float3 start = job.rp0 + mk3(nn.x, nn.y, nn.z) * 0.001f + dv * nn.w;
-                        active = march_begin(m, S, start, dv, int(S.render[1]), S.render[3], 0.0002f);
+                        box_origin = start;
+                        box_exit = tf;
+                        active = march_begin(m, S, start + dv * tn, dv, int(S.render[1]), S.render[3], 0.0002f);
+                        have_d = active && d.w == 2.0f && tn == 0.0f;
+                        known_d = J.contrib.w;
                     }
                     pending = !active;
                 }
@@ -220,8 +264,15 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
         if (!__any_sync(FULL, !retired)) break;
         // One distance evaluation for every lane with a march in flight.
         if (active) {
-            float d = scene_eval<KIND>(S, m.pos, EV_MAP).d;
+            const float d = have_d ? known_d : scene_eval<KIND>(S, m.pos, EV_MAP).d;
+            have_d = false;
             active = march_update(m, S, d, probe);
+            if (active && W.box_on && dot(m.pos - box_origin, m.dir) > box_exit) {
+                // left the box: nothing more to hit; end beyond the far limit (a miss / unoccluded)
+                active = false;
+                m.pos = job.shadow ? job.rp0 + m.dir * (S.render[4] * 1.01f + 1.0f)
+                                   : m.pos + m.dir * (S.render[4] + len3(m.pos - cam) + 1.0f);
+            }
             pending = !active;
         }
         if (pending) {
@@ -454,7 +505,7 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
             }
             if (!terminate && bounce + 1 >= int(S.bounces)) terminate = true;
             emit_march = !terminate;
-            uint32_t nstate = (state & ~0xffu) | uint32_t(bounce + 1) | (terminate ? PF_DONE : 0u);
+            uint32_t nstate = (state & ~(0xffu | PF_KNOWN_D)) | uint32_t(bounce + 1) | (terminate ? PF_DONE : 0u);
             if (terminate) c_paths += 1;
             R.pos = make_float4(hit.x, hit.y, hit.z, side);
             R.dir = make_float4(dr.x, dr.y, dr.z, R.dir.w);

@@ -35,6 +35,12 @@ class FptCudaSkipStats(C.Structure):
                                           "handed_over", "reserved")]
 
 
+class FptCudaRenderStats(C.Structure):
+    _fields_ = [("kernel_launches", C.c_uint64), ("march_launches", C.c_uint64), ("shade_launches", C.c_uint64),
+                ("skip_launches", C.c_uint64), ("march_evals", C.c_uint64), ("shade_evals", C.c_uint64),
+                ("march_ms", C.c_double), ("shade_ms", C.c_double), ("skip_ms", C.c_double), ("total_ms", C.c_double)]
+
+
 MLP_PARAMS = 19777
 
 VOXEL_HIT_DTYPE = np.dtype([("t", np.float32), ("cell", np.uint32), ("normal_axis", np.uint32), ("steps", np.uint32),
@@ -61,9 +67,11 @@ def declare(L: C.CDLL) -> None:
     L.fpt_cuda_mlp_set_params.argtypes = [C.c_uint64, fp, C.c_size_t] + err
     L.fpt_cuda_mlp_gradients.argtypes = [C.c_uint64, fp, C.c_size_t, C.c_float, fp, C.c_size_t, fp] + err
     L.fpt_cuda_skip_stats.argtypes = [P(FptCudaSkipStats)]
+    L.fpt_cuda_render_stats.argtypes = [P(FptCudaRenderStats)]
     for name in ("fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render",
                  "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
-                 "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats"):
+                 "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
+                 "fpt_cuda_render_stats"):
         getattr(L, name).restype = C.c_int
 
 
@@ -216,3 +224,11 @@ def skip_stats() -> dict:
     st = FptCudaSkipStats()
     lib().fpt_cuda_skip_stats(C.byref(st))
     return {k: getattr(st, k) for k, _ in FptCudaSkipStats._fields_ if k != "reserved"}
+
+
+def render_stats() -> dict:
+    """Launch count and per-kernel device times of the last render (times only for profile renders)."""
+    from .native import lib
+    st = FptCudaRenderStats()
+    lib().fpt_cuda_render_stats(C.byref(st))
+    return {k: getattr(st, k) for k, _ in FptCudaRenderStats._fields_}

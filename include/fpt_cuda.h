@@ -558,7 +558,10 @@ enum {
 enum { FPT_CUDA_RNG_HASH13 = 0, FPT_CUDA_RNG_PCG = 1 };
 enum { FPT_CUDA_BRDF_REFERENCE = 0, FPT_CUDA_BRDF_LAMBERT_GGX = 1 };
 enum { FPT_CUDA_NORMAL_CONFIG = 0, FPT_CUDA_NORMAL_ANALYTIC = 1 };
-enum { FPT_CUDA_SURROGATE_OFF = 0, FPT_CUDA_SURROGATE_SKIP = 1 };
+/* SKIP: learned step proposals certified by the exact DE, plus the model's
+ * box (rays are clipped to it; leaving it is a miss).  BOX: the box alone,
+ * no network (the same march without the learned part). */
+enum { FPT_CUDA_SURROGATE_OFF = 0, FPT_CUDA_SURROGATE_SKIP = 1, FPT_CUDA_SURROGATE_BOX = 2 };
 
 /* Scene features beyond FptRenderConfig.  A zero-initialised struct (or a
  * NULL pointer) means the reference's semantics exactly. */
@@ -593,7 +596,7 @@ struct FptCudaSceneExt {
     uint32_t fp64_bisection;     /* 1: FP64 bisection at representable-position stops */
     uint32_t surrogate;          /* FPT_CUDA_SURROGATE_* (needs a trained model) */
     uint64_t surrogate_model;    /* handle from fpt_cuda_mlp_create */
-    float surrogate_margin;      /* exact-DE hand-over distance for surrogate skips */
+    float surrogate_margin;      /* exact-DE hand-over distance for surrogate skips (0: 0.1) */
     float surrogate_safety;      /* step = safety * surrogate distance */
     uint32_t _reserved[8];
 };
@@ -818,6 +821,24 @@ int fpt_cuda_mlp_gradients(uint64_t model,
                            char *error,
                            size_t error_len);
 int fpt_cuda_skip_stats(struct FptCudaSkipStats *stats);
+
+/* Launch and timing record of the last fpt_cuda_render / fpt_metal_render
+ * (no counterpart in the reference).  Kernel times are sums of CUDA-event
+ * spans on the library's stream around each launch; they are recorded only
+ * when the call asked for profile statistics. */
+struct FptCudaRenderStats {
+    uint64_t kernel_launches;    /* kernels launched by the render */
+    uint64_t march_launches;
+    uint64_t shade_launches;
+    uint64_t skip_launches;
+    uint64_t march_evals;        /* DE evaluations in the march kernel (profile renders) */
+    uint64_t shade_evals;        /* normal + material evaluations in the shade kernel (profile renders) */
+    double march_ms;
+    double shade_ms;
+    double skip_ms;
+    double total_ms;             /* the call's elapsed_ms */
+};
+int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
 
 #ifdef __cplusplus
 }

@@ -3,15 +3,18 @@
 * Forward pass and gradients of the BF16 tensor-core kernels against the FP64
   oracle that rounds to BF16 where the kernels store BF16 (the remaining
   differences: FP32 accumulation order, the hardware tanh/sin/cos, BF16
-  rounding-boundary flips).  Tolerances: forward |dy| <= 2e-3 * (max|y| + 0.1)
-  for 99% of points; per parameter block ||g - g_ref|| <= 2e-2 ||g_ref||.
+  rounding-boundary flips; inference takes its sigmoid from an f16x2 tanh).
+  Tolerances: forward |dy| <= 3e-3 * (max|y| + 0.1) for 99% of points;
+  per parameter block ||g - g_ref|| <= 2e-2 ||g_ref||.
 * Training on the GPU lowers the asymmetric loss by 10x and keeps
   overestimates rare.
 * The skip march gives the same hits as the plain march: hit/miss
   agreement >= 99.5% and hit-distance error versus the FP64 oracle within
-  the plain march's own 99th percentile (both within 5e-5 (1 + t)); it
+  1.5x the plain march's own 99th percentile (both within 5e-5 (1 + t)); it
   reports the exact DE evaluations with the trained network, without it
-  (same march, zero network) and without the skip pass.
+  (the same march with the model's box only) and without the skip pass, and
+  checks that the network lowers the exact evaluations below the box-only
+  march.
 """
 import numpy as np
 import pytest
@@ -53,8 +56,8 @@ def test_forward_matches_oracle(blank_model):
     err = np.abs(y - ref)
     scale = np.abs(ref).max() + 0.1
     print(f"forward: max|y| {np.abs(ref).max():.3f} p99 err {np.percentile(err, 99):.2e} max err {err.max():.2e}")
-    assert np.percentile(err, 99) <= 2e-3 * scale
-    assert err.max() <= 1e-2 * scale
+    assert np.percentile(err, 99) <= 3e-3 * scale
+    assert err.max() <= 1.5e-2 * scale
 
 
 def test_gradients_match_oracle(blank_model):
@@ -114,22 +117,16 @@ def test_skip_march_keeps_hits(trained_bulb, native):
     plain, _ = _hits(native, cfg, ext)
     ref = oracle.trace_primary(cfg, ext, fp64=True)
 
-    def run(model):
+    def run(model, mode=1):
         e = scenes.mandelbulb_primary(320, 240)[1]
-        e.surrogate = 1
+        e.surrogate = mode
         e.surrogate_model = model
         hits, _ = _hits(native, cfg, e)
         return hits, nx.skip_stats()
 
     skip, st = run(h)
-    # the same march without the network: a model whose output is zero
-    zero_cfg, zero_ext = scenes.mandelbulb_primary(8, 8)
-    z, _ = nx.mlp_create(zero_cfg, zero_ext, nx.mlp_config(*BULB_BOX, points=0, steps=0))
-    try:
-        nx.mlp_set_params(z, np.zeros(nx.MLP_PARAMS, np.float32))
-        nonet, st0 = run(z)
-    finally:
-        nx.mlp_destroy(z)
+    # the same march without the network: the model's box only
+    nonet, st0 = run(h, mode=2)
     hit_r = ref[..., 5] > 0
     rows = []
     for name, g in (("plain", plain), ("skip", skip), ("no-network", nonet)):
@@ -146,5 +143,26 @@ def test_skip_march_keeps_hits(trained_bulb, native):
     assert e1 <= 5e-5 and e1 <= 1.5 * e0 + 1e-6
     assert e2 <= 5e-5
     assert st["accepted"] > 0 and st["rows"] > 0
+    assert st0["rows"] == 0 and st0["accepted"] == 0
+    assert n1 < n2 < n0   # network < box only < plain
     agree = ((skip["hit"] > 0) == (plain["hit"] > 0)).mean()
     assert agree >= 0.995
+
+
+def test_skip_render_matches_plain(trained_bulb, native):
+    """Path tracing with the skip pass in front of every march pass: same seed, same image as the plain march
+    within sampling noise of paths whose hit points moved by less than the hit threshold."""
+    import ctypes
+    h, _ = trained_bulb
+    b = scenes.mandelbulb_path(256, 144, 8, 4)
+    _, rgba_p, _ = native.cuda_render(b.cfg, b.ext, linear=False)
+    e = type(b.ext)()
+    ctypes.memmove(ctypes.byref(e), ctypes.byref(b.ext), ctypes.sizeof(b.ext))
+    e.surrogate = 1
+    e.surrogate_model = h
+    _, rgba_s, _ = native.cuda_render(b.cfg, e, linear=False)
+    st = nx.skip_stats()
+    m = oracle.image_metrics(rgba_p, rgba_s)
+    print("skip vs plain render:", m, st)
+    assert st["accepted"] > 0 and st["escaped"] > 0
+    assert m["mae"] <= 2.0 and m["lf_ssim"] >= 0.98, m
