@@ -483,7 +483,7 @@ __device__ __forceinline__ Eval mandel_finish(const DeviceScene &S, float3 p, Fi
 template <int KIND> __device__ Field4 mandel_field(float3 p, const DeviceScene &S, int mult) {
     if (KIND == KIND_GENERIC && S.formula == 0) return field_ifs(p, S, mult);
     OrbitResult<float> o;
-    if (KIND == KIND_GENERIC) {
+    if (runtime_kind(KIND)) {
         switch (S.kind) {
             case KIND_BULB8: o = ext_field<KIND_BULB8, float>(S, p.x, p.y, p.z, mult); break;
             case KIND_BULB: o = ext_field<KIND_BULB, float>(S, p.x, p.y, p.z, mult); break;
@@ -746,7 +746,7 @@ __device__ __forceinline__ Eval ext_eval(const DeviceScene &S, float3 p) {
         e = mandel_finish(S, p, mandel_field<KIND>(p, S, 1));
     } else {
         OrbitResult<float> o;
-        switch (KIND == KIND_GENERIC ? S.kind : (uint32_t)KIND) {
+        switch (runtime_kind(KIND) ? S.kind : (uint32_t)KIND) {
             case KIND_BULB8: o = orbit_eval<KIND_BULB8, float>(S, p.x, p.y, p.z, ext_iterations(S), ext_bailout(S)); break;
             case KIND_BULB: o = orbit_eval<KIND_BULB, float>(S, p.x, p.y, p.z, ext_iterations(S), ext_bailout(S)); break;
             case KIND_BOX: o = orbit_eval<KIND_BOX, float>(S, p.x, p.y, p.z, ext_iterations(S), ext_bailout(S)); break;
@@ -831,7 +831,7 @@ static __device__ bool analytic_gradient(const DeviceScene &S, float3 p, float3 
     if (S.formula != 0) {
         D4 x(p.x, 1.f, 0.f, 0.f), y(p.y, 0.f, 1.f, 0.f), z(p.z, 0.f, 0.f, 1.f);
         OrbitResult<D4> o;
-        uint32_t k = KIND == KIND_GENERIC ? S.kind : (uint32_t)KIND;
+        uint32_t k = runtime_kind(KIND) ? S.kind : (uint32_t)KIND;
         switch (k) {
             case KIND_BULB8: o = ext_field<KIND_BULB8, D4>(S, x, y, z, 1); break;
             case KIND_BULB: o = ext_field<KIND_BULB, D4>(S, x, y, z, 1); break;

@@ -15,6 +15,7 @@ struct March {
     float th, step, dist, limit, min_dist, lod_falloff;
     int it, maxi, refine, steps;
     bool refining, found, done;
+    bool stalled;   // ended because a step no longer changed the FP32 position
 };
 
 // sdfMarchIterationLimit: shaders/Shaders.metal:3626-3633
@@ -45,7 +46,7 @@ __device__ __forceinline__ bool march_begin(March &m, const DeviceScene &S, floa
     m.th = 0.0f; m.step = 0.0f; m.dist = 0.0f; m.limit = 1.0f;
     m.min_dist = min_dist; m.lod_falloff = lod_falloff;
     m.it = 0; m.maxi = march_iteration_limit(ni, S); m.refine = 0; m.steps = 0;
-    m.refining = false; m.found = false; m.done = false;
+    m.refining = false; m.found = false; m.done = false; m.stalled = false;
     if (m.maxi <= 0) { m.done = true; return false; }
     return true;
 }
@@ -57,11 +58,11 @@ __device__ __forceinline__ bool mandel_refine_move(March &m) {
     if (m.dist < m.th && m.dist > m.th * m.limit) return march_finish(m, true);
     if (m.dist > m.th) {
         float3 next = m.pos + m.dir * m.step;
-        if (same3(next, m.pos)) return march_finish(m, true);
+        if (same3(next, m.pos)) { m.stalled = true; return march_finish(m, true); }
         m.pos = next;
     } else if (m.dist < m.th * m.limit) {
         float3 next = m.pos - m.dir * m.step;
-        if (same3(next, m.pos)) return march_finish(m, true);
+        if (same3(next, m.pos)) { m.stalled = true; return march_finish(m, true); }
         m.pos = next;
     }
     return true;
@@ -87,7 +88,7 @@ __device__ __forceinline__ bool march_update(March &m, const DeviceScene &S, flo
             }
             m.step = mandel_march_step(d, m.th, S);
             float3 next = m.pos + m.dir * m.step;
-            if (same3(next, m.pos)) return march_finish(m, false);
+            if (same3(next, m.pos)) { m.stalled = true; return march_finish(m, false); }
             m.pos = next;
             if (len3(m.pos - m.start) >= S.render[4]) return march_finish(m, false);
             if (++m.it >= m.maxi) return march_finish(m, false);
@@ -124,6 +125,81 @@ template <int KIND> struct TranslucencyProbe {
         return material_of(*S, e).translucency;
     }
 };
+
+// ---------------------------------------------------------------- FP64 continuation
+// Deep-zoom cameras put the hit threshold below the FP32 resolution of the
+// hit position: marchMandelbulber (shaders/Shaders.metal:3700-3751) then
+// stops where a step no longer changes the position (3726) or where a
+// refinement half-step does (3739-3746).  With DeviceScene::fp64_bisection
+// the ray continues from there in FP64 -- positions along the ray and the
+// extension orbit in double -- with the same step rule, threshold and
+// 30-halving band search as the FP32 march.  Returns the hit distance from
+// `origin` (false: no hit).
+template <int KIND>
+__device__ double de_fp64(const DeviceScene &S, double px, double py, double pz) {
+    OrbitResult<double> o;
+    switch (runtime_kind(KIND) ? S.kind : (uint32_t)KIND) {
+        case KIND_BULB8: o = ext_field<KIND_BULB8, double>(S, px, py, pz, 1); break;
+        case KIND_BULB: o = ext_field<KIND_BULB, double>(S, px, py, pz, 1); break;
+        case KIND_BOX: o = ext_field<KIND_BOX, double>(S, px, py, pz, 1); break;
+        case KIND_MENGER: o = ext_field<KIND_MENGER, double>(S, px, py, pz, 1); break;
+        default: o = ext_field<KIND_HYBRID, double>(S, px, py, pz, 1); break;
+    }
+    return o.escaped ? o.d : -o.d;   // sign carries the escape state for mandel_finish
+}
+
+template <int KIND>
+__device__ bool march_fp64(const DeviceScene &S, float3 origin, float3 dir, double t0, int max_steps, double &t_hit, int &steps) {
+    const double ox = origin.x, oy = origin.y, oz = origin.z;
+    double dx = dir.x, dy = dir.y, dz = dir.z;
+    const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+    dx *= inv; dy *= inv; dz *= inv;
+    const double cx = S.cam_pos[0], cy = S.cam_pos[1], cz = S.cam_pos[2];
+    const float *v = S.vset_values;
+    auto eval = [&](double t, double &th) {
+        const double px = ox + dx * t, py = oy + dy * t, pz = oz + dz * t;
+        const double ex = px - cx, ey = py - cy, ez = pz - cz;
+        th = v[115] > 0.5f ? sqrt(ex * ex + ey * ey + ez * ez) * double(v[116]) : double(v[117]);   // :3635-3641
+        th = fmin(fmax(th, double(v[118])), double(v[119]));
+        double signed_d = de_fp64<KIND>(S, px, py, pz);
+        double d = fabs(signed_d);
+        if (v[115] > 1.5f) {                                                                         // mandel_finish
+            if (signed_d < 0.0) d = 0.0;
+            else if (d < th) d = th * 1.01;
+        }
+        ++steps;
+        return d + (d / 2.0 - d) * double(S.render[6]);
+    };
+    double t = t0, th = 0.0, step = 0.0;
+    double dist = eval(t, th);
+    bool found = false;
+    for (int i = 0; i < max_steps && isfinite(dist); ++i) {
+        if (dist < th) { found = true; break; }
+        step = fmax(dist - 0.5 * th, 0.0) * double(v[113]);                                         // :3643-3681
+        if (v[108] > 0.5f) {
+            step = fmin(fmax(step, double(v[109])), double(v[110]));
+            if (th > v[109]) step = fmin(fmax(step, double(v[111]) * th), double(v[112]) * th);
+        } else {
+            step = fmin(step, double(v[110]));
+        }
+        const double tn = t + step;
+        if (tn == t || tn - t0 >= double(S.render[4])) break;
+        t = tn;
+        dist = eval(t, th);
+    }
+    if (!found) return false;
+    const double limit = 1.0 - 0.001 * fmax(double(v[129]), 0.0);
+    step *= 0.5;
+    for (int r = 0; r < 30; ++r) {                                                                  // :3733-3749
+        if (dist < th && dist > th * limit) break;
+        if (dist > th) t += step;
+        else if (dist < th * limit) t -= step;
+        dist = eval(t, th);
+        step *= 0.5;
+    }
+    t_hit = t;
+    return true;
+}
 
 // Plain-loop march (focus prepass, primary rays, diagnostics).
 template <int KIND>

@@ -97,6 +97,17 @@ __device__ __forceinline__ D4 dmax(D4 a, D4 b) { return a.v >= b.v ? a : b; }
 __device__ __forceinline__ D4 dmin(D4 a, D4 b) { return a.v <= b.v ? a : b; }
 
 // Overload set used by the templated estimators.
+// double overloads serve the FP64 hit-point continuation.
+__device__ __forceinline__ double s_sqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ double s_log(double a) { return log(a); }
+__device__ __forceinline__ double s_abs(double a) { return fabs(a); }
+__device__ __forceinline__ double s_max(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ double s_min(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ double s_val(double a) { return a; }
+__device__ __forceinline__ double s_asin(double a) { return asin(a); }
+__device__ __forceinline__ double s_atan2(double y, double x) { return atan2(y, x); }
+__device__ __forceinline__ double s_pow(double a, float p) { return pow(a, double(p)); }
+__device__ __forceinline__ void s_sincos(double a, double *s, double *c) { sincos(a, s, c); }
 __device__ __forceinline__ float s_sqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ D4 s_sqrt(D4 a) { return dsqrt(a); }
 __device__ __forceinline__ float s_log(float a) { return logf(a); }

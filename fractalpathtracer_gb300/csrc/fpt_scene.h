@@ -21,7 +21,14 @@ enum SceneKind : uint32_t {
     KIND_MENGER = 4,    // Menger fold
     KIND_HYBRID = 5,    // Mandelbulb / Menger hybrid schedule
     KIND_COUNT = 6,
+    KIND_EXT = 6,       // runtime dispatch over the extension formulas only (batched scenes)
 };
+
+// Kinds that pick the formula at run time from DeviceScene::kind.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+constexpr bool runtime_kind(int k) { return k == KIND_GENERIC || k == KIND_EXT; }
 
 struct DeviceScene {
     // --- identity

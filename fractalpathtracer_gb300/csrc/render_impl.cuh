@@ -44,11 +44,25 @@ __global__ void __launch_bounds__(128) trace_primary_kernel(const DeviceScene *s
         March m = march_loop<KIND>(S, rp, dr, int(S.render[1]), S.render[3], 0.0002f);
         float travel = len3(m.pos - rp);
         bool hit = m.found && isfinite(travel) && travel < S.render[4] * 0.99f;
+        int steps = m.steps;
+        float3 hit_pos = m.pos;
+        if (S.fp64_bisection && m.stalled && S.sdf_id == FPT_SDF_MANDELBULBER && S.formula != 0) {
+            // restart a little before the FP32 stop: a few FP32 ulps of the position
+            const float back = 8.0f * 1.1920929e-7f * fmaxf(fmaxf(fabsf(m.pos.x), fabsf(m.pos.y)), fmaxf(fabsf(m.pos.z), 1.0f));
+            double t64 = 0.0;
+            if (march_fp64<KIND>(S, rp, dr, fmax(double(travel) - double(back), 0.0), int(S.render[1]), t64, steps)) {
+                travel = float(t64);
+                hit = travel < S.render[4] * 0.99f;
+                hit_pos = rp + normalize3(dr) * travel;
+            } else {
+                hit = false;
+            }
+        }
         h.distance = travel;
-        h.steps = uint32_t(m.steps);
+        h.steps = uint32_t(steps);
         h.hit = hit ? 1u : 0u;
         if (hit) {
-            float3 n = normal_direct<KIND>(m.pos, S);
+            float3 n = normal_direct<KIND>(hit_pos, S);
             h.normal[0] = n.x; h.normal[1] = n.y; h.normal[2] = n.z;
         }
     }

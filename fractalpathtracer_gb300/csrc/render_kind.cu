@@ -75,7 +75,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         W.wave_base = uint32_t(wb);
         W.n_paths = uint32_t(std::min<uint64_t>(cap, total - wb));
         if ((e = cudaMemsetAsync(W.counters, 0, C_COUNT * sizeof(uint32_t), stream)) != cudaSuccess) return e;
-        camera_kernel<<<std::min<uint32_t>((W.n_paths + 255u) / 256u, uint32_t(sms) * 16u), 256, 0, stream>>>(W);
+        camera_kernel<false><<<std::min<uint32_t>((W.n_paths + 255u) / 256u, uint32_t(sms) * 16u), 256, 0, stream>>>(W);
         ++launches;
         for (uint32_t b = 0; b <= pl.bounces; ++b) {
             const int cur = int(b & 1u);
@@ -88,7 +88,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
             timed(KC_MARCH, [&] { march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur); });
             if (b < pl.bounces) timed(KC_SHADE, [&] { shade_kernel<KIND><<<shade_blocks, 128, 0, stream>>>(W, cur); });
         }
-        finalize_kernel<<<(W.n_paths + 255u) / 256u, 256, 0, stream>>>(W);
+        finalize_kernel<false><<<(W.n_paths + 255u) / 256u, 256, 0, stream>>>(W);
         ++launches;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }

@@ -73,7 +73,24 @@ struct WaveParams {
     // ray enters the box and ends as a miss where it leaves it.
     uint32_t box_on;
     float box_lo[3], box_hi[3];
+    // Batched scenes (multi-scene passes, one sample per pass; null otherwise).
+    // A path's scene is bits 16..31 of its state word.
+    const DeviceScene *scenes;
+    const uint32_t *work_base;   // n_scenes + 1 entries: first work index of each scene
+    const uint32_t *pixel_base;  // n_scenes + 1 entries: first pixel of each scene in accum / sample_rgb
+    uint32_t n_scenes;
+    const uint32_t *pass;        // sample index of the pass (device word, advanced by the pass graph)
 };
+
+// Scene of work index g: the largest k with base[k] <= g (base[0] = 0).
+__device__ __forceinline__ uint32_t batch_scene(const uint32_t *base, uint32_t n, uint32_t g) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= g) lo = mid; else hi = mid;
+    }
+    return lo;
+}
 
 // Forward slab test against the wave's box: [tn, tf] with tn >= 0.
 __device__ __forceinline__ bool wave_box_span(const WaveParams &W, float3 p, float3 d, float &tn, float &tf) {
@@ -131,27 +148,42 @@ __device__ __forceinline__ PathRng path_rng(const DeviceScene &S, uint32_t pixel
 }
 
 // ---------------------------------------------------------------- camera
-static __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
-    const DeviceScene &S = *W.scene;
+template <bool BATCH>
+__global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p - threadIdx.x < W.n_paths; p += gridDim.x * blockDim.x) {
         bool in_wave = p < W.n_paths;
-        uint32_t px = 0, py = 0, s_rel = 0;
+        uint32_t px = 0, py = 0, s_rel = 0, k = 0;
         bool valid = false;
-        if (in_wave) wave_pixel(W, p, S.width, S.height, px, py, s_rel, valid);
+        const DeviceScene *sp = W.scene;
+        if (in_wave) {
+            if (BATCH) {
+                const uint32_t g = W.wave_base + p;
+                k = batch_scene(W.work_base, W.n_scenes, g);
+                sp = W.scenes + k;
+                const uint32_t idx = g - W.work_base[k], tiles_x = (sp->width + 7u) / 8u;
+                const uint32_t tile = idx >> 5, within = idx & 31u;
+                px = (tile % tiles_x) * 8u + (within & 7u);
+                py = (tile / tiles_x) * 4u + (within >> 3);
+                valid = px < sp->width && py < sp->height;
+            } else {
+                wave_pixel(W, p, sp->width, sp->height, px, py, s_rel, valid);
+            }
+        }
+        const DeviceScene &S = *sp;
         bool march = false;
         if (valid) {
             uint32_t pixel = py * S.width + px;
-            uint32_t sample = W.sample_begin + s_rel;
+            uint32_t sample = BATCH ? *W.pass : W.sample_begin + s_rel;
             float2 uv = screen_uv(px, py, S);
             PathRng rng;
             rng.init(S.rng == FPT_CUDA_RNG_PCG, S.seed, pixel, sample, uv.x, uv.y);
             float3 rp, dr;
             PathRec R;
-            uint32_t slot = pixel * W.sample_count + s_rel;
+            uint32_t slot = BATCH ? W.pixel_base[k] + pixel : pixel * W.sample_count + s_rel;
             R.light = make_float4(0.f, 0.f, 0.f, bitsf(slot));
             R.shadow = make_float4(0.f, 0.f, 0.f, 0.f);
             if (!camera_ray(S, uv, rng, true, rp, dr)) {
-                R.color = make_float4(0.f, 0.f, 0.f, bitsf(PF_VALID | PF_DONE | PF_INVISIBLE));
+                R.color = make_float4(0.f, 0.f, 0.f, bitsf(PF_VALID | PF_DONE | PF_INVISIBLE | (k << 16)));
                 R.pos = make_float4(0.f, 0.f, 0.f, 1.f);
                 R.dir = make_float4(0.f, 0.f, 1.f, 0.f);
                 R.grad = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -159,7 +191,7 @@ static __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
                 bool done = S.bounces == 0u;
                 R.pos = make_float4(rp.x, rp.y, rp.z, 1.0f);
                 R.dir = make_float4(dr.x, dr.y, dr.z, 0.0f);
-                R.color = make_float4(1.f, 1.f, 1.f, bitsf(PF_VALID | (done ? PF_DONE : 0u)));
+                R.color = make_float4(1.f, 1.f, 1.f, bitsf(PF_VALID | (done ? PF_DONE : 0u) | (k << 16)));
                 float3 g = background_gradient(dr, S);
                 R.grad = make_float4(g.x, g.y, g.z, 0.f);
                 march = !done;
@@ -182,17 +214,16 @@ struct MarchJob {
     float3 rp0;         // shadow: hit point the ray leaves
 };
 
-template <int KIND>
-__global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
-    const DeviceScene &S = *W.scene;
-    TranslucencyProbe<KIND> probe{W.scene};
+template <int KIND, bool BATCH = false, int BLOCK = 128, int MINB = 7>
+__global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cur) {
+    const DeviceScene *sp = W.scene;   // the lane's scene (per job when BATCH)
     const uint32_t n_path = W.counters[C_MARCH0 + cur];
     const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
     const uint32_t *qm = W.q_march[cur];
     const ShadowJob *qs = W.q_shadow[cur];
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned FULL = 0xffffffffu;
-    const float3 cam = mk3(S.cam_pos[0], S.cam_pos[1], S.cam_pos[2]);
+    float3 cam = BATCH ? mk3(0.0f) : mk3(sp->cam_pos[0], sp->cam_pos[1], sp->cam_pos[2]);
     March m;
     MarchJob job;
     float3 box_origin = mk3(0.0f);   // box mode: ray origin and exit advance of the lane's job
@@ -218,6 +249,11 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
                     const PathRec &R = W.paths[job.path];
                     float4 pos = R.pos, dir = R.dir;
                     uint32_t st = fbits(R.color.w);
+                    if (BATCH) {
+                        sp = W.scenes + (st >> 16);
+                        cam = mk3(sp->cam_pos[0], sp->cam_pos[1], sp->cam_pos[2]);
+                    }
+                    const DeviceScene &S = *sp;
                     job.bounce = st & 0xffu;
                     int ni = job.bounce == 0u ? int(S.render[1]) : int(S.render[1] / (S.render[5] * 2.0f + 1.0f));
                     float3 o = mk3(pos.x, pos.y, pos.z), dv = mk3(dir.x, dir.y, dir.z);
@@ -240,6 +276,11 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
                     float4 o = J.origin, nn = J.normal, d = J.dir;
                     job.path = fbits(o.w);
                     job.shadow = true;
+                    if (BATCH) {
+                        sp = W.scenes + (fbits(W.paths[job.path].color.w) >> 16);
+                        cam = mk3(sp->cam_pos[0], sp->cam_pos[1], sp->cam_pos[2]);
+                    }
+                    const DeviceScene &S = *sp;
                     job.contrib = J.contrib;
                     job.rp0 = mk3(o.x, o.y, o.z);
                     float3 dv = mk3(d.x, d.y, d.z);
@@ -262,6 +303,8 @@ __global__ void __launch_bounds__(128) march_kernel(WaveParams W, int cur) {
             }
         }
         if (!__any_sync(FULL, !retired)) break;
+        const DeviceScene &S = *sp;
+        TranslucencyProbe<KIND> probe{sp};
         // One distance evaluation for every lane with a march in flight.
         if (active) {
             const float d = have_d ? known_d : scene_eval<KIND>(S, m.pos, EV_MAP).d;
@@ -343,12 +386,10 @@ __device__ __forceinline__ void ggx_eval(const DeviceScene &S, float3 n, float3 
     pdf = 0.5f * nl * (1.0f / kPi) + 0.5f * (1.0f / (1.0f + lv)) * D / (4.0f * nv);
 }
 
-template <int KIND>
+template <int KIND, bool BATCH = false>
 __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
-    const DeviceScene &S = *W.scene;
     const int next = cur ^ 1;
     const uint32_t n = W.counters[C_SHADE];
-    const bool ggx = S.brdf == FPT_CUDA_BRDF_LAMBERT_GGX;
     uint32_t c_normal = 0, c_material = 0, c_paths = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += gridDim.x * blockDim.x) {
         bool live = i < n;
@@ -359,10 +400,20 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
             path = W.q_shade[i];
             PathRec R = W.paths[path];
             uint32_t state = fbits(R.color.w);
+            const DeviceScene &S = BATCH ? W.scenes[state >> 16] : *W.scene;
+            const bool ggx = S.brdf == FPT_CUDA_BRDF_LAMBERT_GGX;
             const int bounce = int(state & 0xffu);
             const uint32_t slot = fbits(R.light.w);
-            const uint32_t s_rel = slot % W.sample_count, pixel = slot / W.sample_count;
-            PathRng rng = path_rng(S, pixel, W.sample_begin + s_rel);
+            uint32_t pixel, sample;
+            if (BATCH) {
+                pixel = slot - W.pixel_base[state >> 16];
+                sample = *W.pass;
+            } else {
+                const uint32_t s_rel = slot % W.sample_count;
+                pixel = slot / W.sample_count;
+                sample = W.sample_begin + s_rel;
+            }
+            PathRng rng = path_rng(S, pixel, sample);
             float3 hit = mk3(R.pos.x, R.pos.y, R.pos.z), dr = mk3(R.dir.x, R.dir.y, R.dir.z);
             float3 color = mk3(R.color.x, R.color.y, R.color.z), light = mk3(R.light.x, R.light.y, R.light.z);
             float side = R.pos.w;
@@ -531,6 +582,24 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
     }
 }
 
+// One pass of a batch: accum = mix(accum, sample, 1 / (pass + 1)) over every
+// pixel of every scene (the in-order mean of reduce_samples_kernel, one
+// sample at a time), then the pass index advances for the next replay.
+static __global__ void __launch_bounds__(256) reduce_pass_kernel(const float4 *sample_rgb, float4 *accum, uint32_t pixels,
+                                                                 const uint32_t *pass) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= pixels) return;
+    const uint32_t i = *pass;
+    float3 mean = mk3(0.0f);
+    if (i > 0u) { const float4 a = accum[p]; mean = mk3(a.x, a.y, a.z); }
+    const float4 c = sample_rgb[p];
+    mean = mix3(mean, mk3(c.x, c.y, c.z), 1.0f / float(i + 1u));
+    accum[p] = make_float4(mean.x, mean.y, mean.z, 1.0f);
+}
+static __global__ void advance_pass_kernel(uint32_t *pass) {
+    if (threadIdx.x == 0) *pass += 1u;
+}
+
 // Resets the counters the next pass appends to.
 static __global__ void reset_counters_kernel(uint32_t *counters, int next) {
     if (threadIdx.x == 0) {
@@ -545,13 +614,14 @@ static __global__ void reset_counters_kernel(uint32_t *counters, int next) {
 // Path colour: (light + sun light) times throughput (reference estimator)
 // or the throughput-weighted sum (extension estimator), gradient mix and
 // the 8.0 clamp of renderPath (shaders/Shaders.metal:6023-6025).
-static __global__ void __launch_bounds__(256) finalize_kernel(WaveParams W) {
-    const DeviceScene &S = *W.scene;
+template <bool BATCH>
+__global__ void __launch_bounds__(256) finalize_kernel(WaveParams W) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= W.n_paths) return;
     const PathRec &R = W.paths[p];
     uint32_t state = fbits(R.color.w);
     if (!(state & PF_VALID)) return;
+    const DeviceScene &S = BATCH ? W.scenes[state >> 16] : *W.scene;
     float3 col = mk3(0.0f);
     if (!(state & PF_INVISIBLE)) {
         float3 light = mk3(R.light.x + R.shadow.x, R.light.y + R.shadow.y, R.light.z + R.shadow.z);

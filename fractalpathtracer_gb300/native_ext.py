@@ -41,6 +41,23 @@ class FptCudaRenderStats(C.Structure):
                 ("march_ms", C.c_double), ("shade_ms", C.c_double), ("skip_ms", C.c_double), ("total_ms", C.c_double)]
 
 
+class FptCudaBatchStats(C.Structure):
+    _fields_ = [("elapsed_ms", C.c_double), ("build_ms", C.c_double), ("paths", C.c_uint64), ("scenes", C.c_uint32),
+                ("passes", C.c_uint32), ("graph_launches", C.c_uint32), ("kernel_launches_per_pass", C.c_uint32),
+                ("block_size", C.c_uint32), ("registers", C.c_uint32), ("wave_paths", C.c_uint32), ("tuned", C.c_uint32),
+                ("workload_key", C.c_uint64)]
+
+
+class FptCudaTuneCandidate(C.Structure):
+    _fields_ = [("block_size", C.c_uint32), ("registers", C.c_uint32), ("wave_paths", C.c_uint32), ("_pad", C.c_uint32),
+                ("median_ms", C.c_double)]
+
+
+class FptCudaTuneResult(C.Structure):
+    _fields_ = [("candidates", C.c_uint32), ("chosen", C.c_uint32), ("rounds", C.c_uint32), ("_pad", C.c_uint32),
+                ("workload_key", C.c_uint64), ("tried", FptCudaTuneCandidate * 16)]
+
+
 MLP_PARAMS = 19777
 
 VOXEL_HIT_DTYPE = np.dtype([("t", np.float32), ("cell", np.uint32), ("normal_axis", np.uint32), ("steps", np.uint32),
@@ -68,10 +85,13 @@ def declare(L: C.CDLL) -> None:
     L.fpt_cuda_mlp_gradients.argtypes = [C.c_uint64, fp, C.c_size_t, C.c_float, fp, C.c_size_t, fp] + err
     L.fpt_cuda_skip_stats.argtypes = [P(FptCudaSkipStats)]
     L.fpt_cuda_render_stats.argtypes = [P(FptCudaRenderStats)]
+    L.fpt_cuda_render_batch.argtypes = [cfg, ext, C.c_size_t, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_size_t,
+                                        P(FptCudaBatchStats)] + err
+    L.fpt_cuda_autotune_batch.argtypes = [cfg, ext, C.c_size_t, C.c_uint32, P(FptCudaTuneResult)] + err
     for name in ("fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render",
                  "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
                  "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
-                 "fpt_cuda_render_stats"):
+                 "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch"):
         getattr(L, name).restype = C.c_int
 
 
@@ -232,3 +252,49 @@ def render_stats() -> dict:
     st = FptCudaRenderStats()
     lib().fpt_cuda_render_stats(C.byref(st))
     return {k: getattr(st, k) for k, _ in FptCudaRenderStats._fields_}
+
+
+# ---------------------------------------------------------------- batched scenes
+def _batch_arrays(bundles):
+    n = len(bundles)
+    cfgs = (ffi.FptRenderConfig * n)()
+    exts = (ffi.FptCudaSceneExt * n)()
+    for k, b in enumerate(bundles):
+        C.memmove(C.byref(cfgs[k]), C.byref(b.cfg), C.sizeof(ffi.FptRenderConfig))
+        C.memmove(C.byref(exts[k]), C.byref(b.ext), C.sizeof(ffi.FptCudaSceneExt))
+    return cfgs, exts
+
+
+def render_batch(bundles, linear=True, rgba=False):
+    """fpt_cuda_render_batch: per scene (H, W, 4) float32 accumulation (and uint8 images), plus stats."""
+    from .native import lib
+    cfgs, exts = _batch_arrays(bundles)
+    sizes = [(b.cfg.height, b.cfg.width) for b in bundles]
+    total = sum(h * w for h, w in sizes)
+    lin = np.zeros(total * 4, np.float32) if linear else None
+    img = np.zeros(total * 4, np.uint8) if rgba else None
+    st = FptCudaBatchStats()
+    e = _err()
+    _check(lib().fpt_cuda_render_batch(cfgs, exts, len(bundles),
+                                       lin.ctypes.data_as(C.POINTER(C.c_float)) if lin is not None else None,
+                                       lin.size if lin is not None else 0,
+                                       img.ctypes.data_as(C.POINTER(C.c_uint8)) if img is not None else None,
+                                       img.size if img is not None else 0, C.byref(st), e, len(e)), e)
+    out_lin, out_img, off = [], [], 0
+    for h, w in sizes:
+        if lin is not None:
+            out_lin.append(lin[off * 4:(off + h * w) * 4].reshape(h, w, 4))
+        if img is not None:
+            out_img.append(img[off * 4:(off + h * w) * 4].reshape(h, w, 4))
+        off += h * w
+    return out_lin, out_img, {k: getattr(st, k) for k, _ in FptCudaBatchStats._fields_}
+
+
+def autotune_batch(bundles, rounds=3) -> dict:
+    from .native import lib
+    cfgs, exts = _batch_arrays(bundles)
+    r = FptCudaTuneResult()
+    e = _err()
+    _check(lib().fpt_cuda_autotune_batch(cfgs, exts, len(bundles), rounds, C.byref(r), e, len(e)), e)
+    tried = [{k: getattr(r.tried[i], k) for k, _ in FptCudaTuneCandidate._fields_ if k != "_pad"} for i in range(r.candidates)]
+    return {"chosen": r.chosen, "rounds": r.rounds, "workload_key": r.workload_key, "tried": tried}

@@ -285,6 +285,64 @@ def mandelbox_path(width: int = 1920, height: int = 1080, spp: int = 16, bounces
     return _fractal_path(mandelbox_ext(), width, height, spp, bounces, seed, (0.0, 1.5, -7.0), (0.0, 0.0, 0.0), 1e-4 / 7.0)
 
 
+def hybrid_ext(power: float = 8.0, iterations: int = 9, menger_scale: float = 3.0, period: int = 3,
+               bailout: float = 4.0) -> ffi.FptCudaSceneExt:
+    """Mandelbulb / Menger-fold hybrid: every period-th iteration is a Menger fold (2:1 for period 3)."""
+    e = ffi.FptCudaSceneExt()
+    e.formula = ffi.FORMULA_BULB_MENGER_HYBRID
+    e.power = power
+    e.iterations = iterations
+    e.menger_scale = menger_scale
+    e.hybrid_period = period
+    e.bailout = bailout
+    e.normal_mode = ffi.NORMAL_ANALYTIC
+    return e
+
+
+def mandelbulb_deep_zoom(eye, target, width: int = 64, height: int = 48, fov_deg: float = 0.05,
+                         threshold_per_unit: float = 1e-7, fp64: bool = True):
+    """Deep-zoom primary rays on the power-8 Mandelbulb: a camera a short way off the surface with a tiny field of
+    view, so the hit threshold (pixel footprint) falls below the FP32 resolution of the hit position; `fp64` turns
+    on the FP64 hit-point continuation."""
+    cfg, ext = mandelbulb_primary(width, height)
+    cfg.camera_fov = fov_for_vertical(fov_deg)
+    look_at(cfg, eye, target)
+    _mandelbulber_march(cfg, threshold_per_unit, 2000, 10.0)
+    cfg.vset_values[118] = 1e-14      # threshold clamp below the zoom's footprint
+    cfg.vset_values[109] = 1e-15
+    cfg.set_values[1] = 8.0
+    cfg.set_values[2] = 2.0
+    ext.fp64_bisection = 1 if fp64 else 0
+    return cfg, ext
+
+
+def batch_scene(k: int, spp: int = 4, bounces: int = 3) -> SceneBundle:
+    """Scene k of the batched workload, drawn from a PCG64 stream seeded by k: a Mandelbulb (power
+    U[2, 12]), a Mandelbox (scale U[-2.5, -1.5]) or a 2:1 Mandelbulb / Menger hybrid; iterations U{4..16};
+    square image with a log-uniform side in [64, 512]; seeded camera azimuth."""
+    rng = np.random.default_rng(k)
+    kind = int(rng.integers(3))
+    iters = int(rng.integers(4, 17))
+    side = int(round(math.exp(rng.uniform(math.log(64.0), math.log(512.0)))))
+    az = rng.uniform(0.0, 2.0 * math.pi)
+    if kind == 0:
+        ext = mandelbulb_ext(power=float(rng.uniform(2.0, 12.0)), iterations=iters, bailout=2.0)
+        dist, thr = 3.0, 1e-4 / 3.0
+    elif kind == 1:
+        ext = mandelbox_ext(scale=float(rng.uniform(-2.5, -1.5)), iterations=iters)
+        dist, thr = 7.0, 1e-4 / 7.0
+    else:
+        ext = hybrid_ext(iterations=iters)
+        dist, thr = 3.5, 1e-4 / 3.5
+    eye = (dist * math.sin(az), 0.25 * dist, -dist * math.cos(az))
+    return _fractal_path(ext, side, side, spp, bounces, k + 1, eye, (0.0, 0.0, 0.0), thr)
+
+
+def batch_scenes(count: int = 64, spp: int = 4, bounces: int = 3):
+    """The batched workload: scenes 0..count-1 of batch_scene."""
+    return [batch_scene(k, spp, bounces) for k in range(count)]
+
+
 # Boxes holding all of each surrogate scene's surface (the power-8 Mandelbulb
 # reaches |x| ~ 1.11, the scale -1.5 Mandelbox |x| ~ 2.01): the skip march
 # treats rays leaving them as misses.

@@ -840,6 +840,68 @@ struct FptCudaRenderStats {
 };
 int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
 
+/* ---- Batched scenes (no counterpart in the reference; its render-batch
+ * command only reuses the process, src/main.rs:2269) ----
+ * count scenes (extension formulas, the same sample count, no sky image, no
+ * surrogate) of any size and iteration count render together: every spp
+ * pass covers all scenes with one persistent launch per march pass, and the
+ * pass is one CUDA graph replayed spp times.  Each scene's image equals its
+ * fpt_cuda_render image at the same seed.  Outputs are concatenated in scene
+ * order: linear_output W_k*H_k*4 floats per scene (accumulation buffer, row
+ * 0 = bottom), rgba_output W_k*H_k*4 bytes per scene (top row first).  The
+ * launch shape comes from fpt_cuda_autotune_batch when it tuned the same
+ * workload key, else the default. */
+struct FptCudaBatchStats {
+    double elapsed_ms;           /* graph replays (all passes), CUDA events */
+    double build_ms;             /* graph capture + instantiation */
+    uint64_t paths;              /* sum of W*H*spp */
+    uint32_t scenes;
+    uint32_t passes;
+    uint32_t graph_launches;
+    uint32_t kernel_launches_per_pass;
+    uint32_t block_size;         /* march kernel */
+    uint32_t registers;          /* march kernel registers per thread */
+    uint32_t wave_paths;         /* paths per wave */
+    uint32_t tuned;              /* 1 when the autotuner's choice was used */
+    uint64_t workload_key;
+};
+int fpt_cuda_render_batch(const struct FptRenderConfig *configs,
+                          const struct FptCudaSceneExt *exts,
+                          size_t count,
+                          float *linear_output,
+                          size_t linear_output_len,
+                          uint8_t *rgba_output,
+                          size_t rgba_output_len,
+                          struct FptCudaBatchStats *stats,
+                          char *error,
+                          size_t error_len);
+
+struct FptCudaTuneCandidate {
+    uint32_t block_size;
+    uint32_t registers;
+    uint32_t wave_paths;
+    uint32_t _pad;
+    double median_ms;            /* median render time over the timed rounds */
+};
+struct FptCudaTuneResult {
+    uint32_t candidates;
+    uint32_t chosen;             /* index into tried; 0 is the default shape */
+    uint32_t rounds;
+    uint32_t _pad;
+    uint64_t workload_key;
+    struct FptCudaTuneCandidate tried[16];
+};
+/* Times every launch-shape candidate on this batch (one warm-up, then
+ * `rounds` interleaved rounds), keeps the fastest when it beats the default
+ * by 3%, and remembers the choice for the batch's workload key. */
+int fpt_cuda_autotune_batch(const struct FptRenderConfig *configs,
+                            const struct FptCudaSceneExt *exts,
+                            size_t count,
+                            uint32_t rounds,
+                            struct FptCudaTuneResult *result,
+                            char *error,
+                            size_t error_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,3 +42,20 @@ def test_unsupported_entries_fail_cleanly_without_gpu(native):
     assert b"unsupported" in err.value
     stats = ffi.FptAsyncJitStats()
     assert lib.fpt_test_async_stitch_context(b"", b"", b"", None, C.byref(stats), err, len(err)) == 1
+
+
+def test_batch_scene_generator_is_seeded():
+    from fractalpathtracer_gb300 import ffi, scenes
+    a = scenes.batch_scenes(64)
+    b = scenes.batch_scenes(64)
+    kinds = set()
+    for x, y in zip(a, b):
+        assert bytes(x.cfg) == bytes(y.cfg) and bytes(x.ext) == bytes(y.ext)
+        assert 64 <= x.cfg.width <= 512 and x.cfg.width == x.cfg.height
+        assert 4 <= x.ext.iterations <= 16 and x.cfg.samples == 4 and x.cfg.render[0] == 3.0
+        kinds.add(x.ext.formula)
+        if x.ext.formula == ffi.FORMULA_MANDELBULB:
+            assert 2.0 <= x.ext.power <= 12.0
+        if x.ext.formula == ffi.FORMULA_MANDELBOX:
+            assert -2.5 <= x.ext.box_scale <= -1.5
+    assert kinds == {ffi.FORMULA_MANDELBULB, ffi.FORMULA_MANDELBOX, ffi.FORMULA_BULB_MENGER_HYBRID}
