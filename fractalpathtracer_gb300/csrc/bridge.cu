@@ -23,6 +23,7 @@
 #include "image_io.h"
 #include "bridge_internal.h"
 #include "skip.cuh"
+#include "diag.cuh"
 
 namespace fpt {
 
@@ -226,6 +227,11 @@ bool compile_scene(const FptRenderConfig &c, const FptCudaSceneExt *ext_in, Devi
     S.shading_count = std::min<uint32_t>(c.sdf_shading_program_count, FPT_SDF_PROGRAM_MAX_OPS);
     std::memcpy(S.program, c.sdf_program, sizeof(S.program));
     std::memcpy(S.shading, c.sdf_shading_program, sizeof(S.shading));
+    S.soa = c.sdf_typed_soa;
+    S.soa.sphere_count = std::min<uint32_t>(S.soa.sphere_count, FPT_SDF_FLAT_UNION_MAX_PRIMITIVES);
+    S.soa.box_count = std::min<uint32_t>(S.soa.box_count, FPT_SDF_FLAT_UNION_MAX_PRIMITIVES);
+    S.soa.plane_count = std::min<uint32_t>(S.soa.plane_count, FPT_SDF_FLAT_UNION_MAX_PRIMITIVES);
+    S.soa_count = S.program_count > 0u ? S.soa.sphere_count + S.soa.box_count + S.soa.plane_count : 0u;
     return true;
 }
 
@@ -656,6 +662,117 @@ int fpt_cuda_render_stats(struct FptCudaRenderStats *stats) {
     if (!stats) return 1;
     std::lock_guard<std::mutex> lock(ctx().mutex);
     *stats = ctx().last_render;
+    return 0;
+}
+
+// Diagnostic images (src/metal_bridge.mm:5865-6025; kernel shaders/Shaders.metal:7290-7385): the encoded
+// quantity of every pixel written as a PNG at output_path.
+int fpt_metal_diagnostic_render(const char *metallib_path, const char *output_path, const char *shader_source,
+                                size_t shader_source_len, const struct FptRenderConfig *config,
+                                const struct FptDiagnosticConfig *diagnostic, double *elapsed_ms, char *error, size_t error_len) {
+    (void)metallib_path; (void)shader_source; (void)shader_source_len;
+    if (elapsed_ms) *elapsed_ms = 0.0;
+    if (!config || !diagnostic) { set_error(error, error_len, "missing diagnostic render config"); return 1; }
+    if (!output_path) { set_error(error, error_len, "missing diagnostic output path"); return 1; }
+    if (config->width == 0 || config->height == 0) {
+        set_error(error, error_len, "invalid render size %ux%u", config->width, config->height);
+        return 1;
+    }
+    const uint32_t mode = diagnostic->mode;
+    if (mode > DIAG_SDF_BOUNCE_CONTRIBUTION) { set_error(error, error_len, "unknown diagnostic mode %u", mode); return 1; }
+    if (mode == DIAG_SDF_BOUNCE_CONTRIBUTION) {
+        set_error(error, error_len, "diagnostic mode %u (bounce contribution) is not supported by the CUDA path", mode);
+        return 1;
+    }
+    if (config->renderer_backend != FPT_RENDERER_SDF) {
+        set_error(error, error_len, "diagnostic images of renderer backend %u are not supported by the CUDA path", config->renderer_backend);
+        return 1;
+    }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    FptRenderConfig hydrated = *config;
+    if (!hydrate_hdri(hydrated, error, error_len)) return 1;
+    const size_t pixels = size_t(hydrated.width) * hydrated.height;
+    float ms = 0.0f;
+    if (mode == DIAG_PATH_FINAL) {
+        // the path-traced mean of min(max(spp, 16), 64) samples through postProcess
+        FptRenderConfig r = hydrated;
+        r.samples = std::min(std::max(r.samples, 16u), 64u);
+        double rms = 0.0;
+        if (render_core(&r, nullptr, nullptr, nullptr, 0, nullptr, 0, &rms, nullptr, nullptr, nullptr, nullptr, nullptr, error,
+                        error_len))
+            return 1;
+        DeviceScene S;
+        if (!compile_scene(r, nullptr, S, error, error_len)) return 1;
+        if (!check(launch_diag_final(c.scene, S.width, S.height, c.accum, c.rgba, c.stream), "diagnostic present", error, error_len) ||
+            !check(cudaStreamSynchronize(c.stream), "diagnostic present", error, error_len))
+            return 1;
+        ms = float(rms);
+    } else {
+        DeviceScene S;
+        if (!compile_scene(hydrated, nullptr, S, error, error_len)) return 1;
+        if (!upload_scene(S, nullptr, error, error_len)) return 1;
+        if (!ensure_buffer((void **)&c.rgba, &c.cap_rgba, pixels * sizeof(uchar4), error, error_len)) return 1;
+        cudaEventRecord(c.ev0, c.stream);
+        if (hydrated.focus_distance <= 0.0f &&
+            !check(launch_focus(S.kind, c.scene, c.stream), "focus-distance prepass", error, error_len))
+            return 1;
+        if (!check(launch_diagnostic(S.kind, c.scene, S.width, S.height, mode, diagnostic->max_distance, c.rgba, c.stream),
+                   "diagnostic launch", error, error_len))
+            return 1;
+        cudaEventRecord(c.ev1, c.stream);
+        if (!check(cudaStreamSynchronize(c.stream), "diagnostic render", error, error_len)) return 1;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    }
+    if (elapsed_ms) *elapsed_ms = ms;
+    std::vector<uint8_t> rgba(pixels * 4);
+    if (!check(cudaMemcpy(rgba.data(), c.rgba, pixels * 4, cudaMemcpyDeviceToHost), "diagnostic readback", error, error_len)) return 1;
+    std::string err;
+    if (!write_png(output_path, hydrated.width, hydrated.height, rgba.data(), err)) {
+        set_error(error, error_len, "%s", err.c_str());
+        return 1;
+    }
+    return 0;
+}
+
+// Typed SoA validation (src/metal_bridge.mm:4116-4200): the lowered program
+// (config->sdf_typed_soa) against the interpreter on 2^20 points.
+int fpt_test_typed_soa(const char *metallib_path, const struct FptRenderConfig *config, struct FptStitchValidationStats *stats,
+                       char *error, size_t error_len) {
+    (void)metallib_path;
+    if (!config || !stats) { set_error(error, error_len, "missing typed-SoA validation input"); return 1; }
+    std::memset(stats, 0, sizeof(*stats));
+    const uint32_t prims = config->sdf_typed_soa.sphere_count + config->sdf_typed_soa.box_count + config->sdf_typed_soa.plane_count;
+    if (config->sdf_id != FPT_SDF_PROGRAM || prims == 0u || config->sdf_program_count == 0u) {
+        set_error(error, error_len, "typed-SoA validation requires a lowered typed program");
+        return 1;
+    }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    DeviceScene S;
+    if (!compile_scene(*config, nullptr, S, error, error_len) || !upload_scene(S, nullptr, error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len) ||
+        !check(cudaMemsetAsync(c.counter, 0, 4 * sizeof(unsigned int), c.stream), "counter reset", error, error_len))
+        return 1;
+    const uint32_t n = 1u << 20;
+    unsigned int counts[4] = {0, 0, 0, 0};
+    if (!check(launch_typed_soa_validation(c.scene, config->voxel_bounds_min, config->voxel_bounds_max, n, c.counter, c.stream),
+               "typed-SoA validation launch", error, error_len) ||
+        !check(cudaMemcpyAsync(counts, c.counter, sizeof(counts), cudaMemcpyDeviceToHost, c.stream), "counts readback", error,
+               error_len) ||
+        !check(cudaStreamSynchronize(c.stream), "typed-SoA validation", error, error_len))
+        return 1;
+    stats->sample_count = n;
+    stats->distance_failures = counts[0];
+    stats->gradient_failures = counts[1];
+    std::memcpy(&stats->max_distance_error, &counts[2], sizeof(float));
+    std::memcpy(&stats->max_gradient_error, &counts[3], sizeof(float));
+    if (counts[0] != 0u || counts[1] != 0u) {
+        set_error(error, error_len, "typed-SoA validation failed: %u distance, %u gradient", counts[0], counts[1]);
+        return 1;
+    }
     return 0;
 }
 

@@ -562,6 +562,59 @@ static __device__ Eval program_distance(float3 p, const DeviceScene &S, bool sha
     }
     return {distance, orbit, 0};
 }
+// Typed SoA direct evaluation (deTypedSoADistance / typedSoASurface,
+// :2857-2960): the union of the lowered spheres, boxes and planes without the
+// interpreter.  The surface form also returns the winner's gradient; equal
+// distances go to the primitive with the lower source instruction.
+__device__ __forceinline__ float soa_distance(float3 p, const DeviceScene &S) {
+    const FptTypedSoAProgram &T = S.soa;
+    float d = kInf;
+    for (uint32_t i = 0; i < T.sphere_count; ++i)
+        d = fminf(d, len3(p - mk3(T.sphere_x[i], T.sphere_y[i], T.sphere_z[i])) - T.sphere_radius[i]);
+    for (uint32_t i = 0; i < T.box_count; ++i) {
+        float3 q = abs3(p - mk3(T.box_x[i], T.box_y[i], T.box_z[i])) - mk3(T.box_half_x[i], T.box_half_y[i], T.box_half_z[i]);
+        d = fminf(d, fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.0f) + len3(max3(q, mk3(0.0f))));
+    }
+    for (uint32_t i = 0; i < T.plane_count; ++i) {
+        float3 n = normalize3(mk3(T.plane_x[i], T.plane_y[i], T.plane_z[i]));
+        d = fminf(d, dot(p - mk3(T.plane_center_x[i], T.plane_center_y[i], T.plane_center_z[i]), n) + T.plane_offset[i]);
+    }
+    return d;
+}
+__device__ __forceinline__ float soa_surface(float3 p, const DeviceScene &S, float3 &g) {
+    const FptTypedSoAProgram &T = S.soa;
+    float best = kInf;
+    uint32_t src = 0xffffffffu;
+    g = mk3(0.0f);
+    auto take = [&](float cand, uint32_t s, float3 grad) {
+        if (cand < best || (cand == best && s < src)) { best = cand; src = s; g = grad; }
+    };
+    for (uint32_t i = 0; i < T.sphere_count; ++i) {
+        float3 l = p - mk3(T.sphere_x[i], T.sphere_y[i], T.sphere_z[i]);
+        float r = len3(l);
+        take(r - T.sphere_radius[i], T.sphere_source[i], r > 1.0e-8f ? l / r : mk3(0.f, 1.f, 0.f));
+    }
+    for (uint32_t i = 0; i < T.box_count; ++i) {
+        float3 l = p - mk3(T.box_x[i], T.box_y[i], T.box_z[i]);
+        float3 q = abs3(l) - mk3(T.box_half_x[i], T.box_half_y[i], T.box_half_z[i]);
+        float3 o = max3(q, mk3(0.0f));
+        float ol = len3(o);
+        float cand = fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.0f) + ol;
+        float3 grad;
+        if (ol > 1.0e-8f) grad = mk3(signf(l.x) * o.x, signf(l.y) * o.y, signf(l.z) * o.z) / ol;
+        else if (q.x >= q.y && q.x >= q.z) grad = mk3(signf(l.x), 0.f, 0.f);
+        else if (q.y >= q.z) grad = mk3(0.f, signf(l.y), 0.f);
+        else grad = mk3(0.f, 0.f, signf(l.z));
+        take(cand, T.box_source[i], grad);
+    }
+    for (uint32_t i = 0; i < T.plane_count; ++i) {
+        float3 n = normalize3(mk3(T.plane_x[i], T.plane_y[i], T.plane_z[i]));
+        take(dot(p - mk3(T.plane_center_x[i], T.plane_center_y[i], T.plane_center_z[i]), n) + T.plane_offset[i],
+             T.plane_source[i], n);
+    }
+    return best;
+}
+
 // programSurfaceInterpreted: Jacobian-propagated gradient (:3266-3369).
 static __device__ float3 program_gradient(float3 p, const DeviceScene &S, float *dist_out) {
     float3 jx = mk3(1.f, 0.f, 0.f), jy = mk3(0.f, 1.f, 0.f), jz = mk3(0.f, 0.f, 1.f);
@@ -777,6 +830,7 @@ __device__ __forceinline__ Eval scene_eval(const DeviceScene &S, float3 p, int m
     } else {
         switch (S.sdf_id) {
             case FPT_SDF_PROGRAM:
+                if (S.soa_count > 0u && mode != EV_MATERIAL) { e = {soa_distance(p, S), 0.0f, 0}; break; }   // :3576-3578
                 if (S.program_count > 0u) { e = program_distance(p, S, mode == EV_MATERIAL); break; }
                 e = {1000.0f, 0.0f, 0}; break;
             case FPT_SDF_README_CORNELL: e = readme_scene(p, false); break;
@@ -844,7 +898,8 @@ static __device__ bool analytic_gradient(const DeviceScene &S, float3 p, float3 
         return true;
     }
     if (S.sdf_id == FPT_SDF_PROGRAM && S.program_count > 0u && (S.normal_mode == 0u || S.normal_mode == 2u)) {
-        g = program_gradient(p, S, nullptr);
+        if (S.soa_count > 0u) soa_surface(p, S, g);   // programSurface uses the lowered form (:3403-3405)
+        else g = program_gradient(p, S, nullptr);
         return dot(g, g) >= 1.0e-12f && finite3(g);
     }
     return false;

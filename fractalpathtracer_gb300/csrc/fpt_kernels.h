@@ -64,6 +64,13 @@ cudaError_t launch_sample_distance(uint32_t kind, const DeviceScene *scene, cons
 cudaError_t launch_label(uint32_t kind, const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t stream);
 cudaError_t launch_skip_primary(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, const SkipArgs &args,
                                 FptCudaPrimaryHit *hits, cudaStream_t stream);
+// Diagnostic image (modes of FptDiagnosticConfig except 7 and 15) and the mode-7 present.
+cudaError_t launch_diagnostic(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, uint32_t mode, float max_distance,
+                              uchar4 *out, cudaStream_t stream);
+cudaError_t launch_diag_final(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out, cudaStream_t stream);
+// Typed SoA vs interpreter over n hash-seeded points; counts[4] as in the kernel.
+cudaError_t launch_typed_soa_validation(const DeviceScene *scene, const float bmin[3], const float bmax[3], uint32_t n,
+                                        unsigned int *counts, cudaStream_t stream);
 cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out,
                            cudaStream_t stream);
 

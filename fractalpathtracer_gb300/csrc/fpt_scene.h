@@ -103,6 +103,10 @@ struct DeviceScene {
 
     // --- typed programs
     uint32_t program_count, shading_count;
+    // Typed program lowered to flat arrays (sdf_typed_soa; the lowering is the
+    // host's, src/scene.rs:1211-1531): spheres, boxes and planes in one union.
+    uint32_t soa_count;            // 0: not lowered
+    FptTypedSoAProgram soa;
     FptSdfInstruction program[FPT_SDF_PROGRAM_MAX_OPS];
     FptSdfInstruction shading[FPT_SDF_PROGRAM_MAX_OPS];
 };

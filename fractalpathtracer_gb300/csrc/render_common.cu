@@ -1,5 +1,6 @@
 // render_common.cu -- present kernel and the per-kind dispatch of the launchers.
 #include "render_impl.cuh"
+#include "fpt_post.cuh"
 
 namespace fpt {
 
@@ -7,39 +8,6 @@ namespace fpt {
 // present_kernel (shaders/Shaders.metal:8012-8025) with highlightAt
 // (7466-7481), sampleAccumBilinear (7483-7496), chromaticAt (7498-7507),
 // postProcess/toneMap (6778-6825) and the vertical flip of outputIndex.
-__device__ __forceinline__ float3 gamma_srgb(float3 l) {
-    float3 o;
-    o.x = l.x <= 0.0031308f ? l.x * 12.92f : 1.055f * powf(fmaxf(l.x, 0.0f), 1.0f / 2.4f) - 0.055f;
-    o.y = l.y <= 0.0031308f ? l.y * 12.92f : 1.055f * powf(fmaxf(l.y, 0.0f), 1.0f / 2.4f) - 0.055f;
-    o.z = l.z <= 0.0031308f ? l.z * 12.92f : 1.055f * powf(fmaxf(l.z, 0.0f), 1.0f / 2.4f) - 0.055f;
-    return o;
-}
-__device__ __forceinline__ float aces1(float x) { return clampf((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f, 1.0f); }
-__device__ float3 pbr_neutral(float3 c) {
-    float x = fminf(c.x, fminf(c.y, c.z));
-    float off = x < 0.08f ? x - 6.25f * x * x : 0.04f;
-    c = c - off;
-    float peak = maxc3(c);
-    if (peak < 0.76f) return c;
-    float d = 1.0f - 0.76f;
-    float np = 1.0f - d * d / (peak + d - 0.76f);
-    c = c * (np / peak);
-    float g = 1.0f - 1.0f / (0.15f * (peak - np) + 1.0f);
-    return mix3(c, mk3(np), g);
-}
-__device__ float3 post_process(float3 c, const DeviceScene &S) {
-    float n = S.post[0];
-    if (n == 0.0f) c = gamma_srgb(c);
-    else if (n == 1.0f) c = mk3(powf(c.x, 1.0f / 2.4f), powf(c.y, 1.0f / 2.4f), powf(c.z, 1.0f / 2.4f));
-    else if (n == 2.0f) c = mk3(powf(c.x, 1.0f / 2.6f), powf(c.y, 1.0f / 2.6f), powf(c.z, 1.0f / 2.6f));
-    else if (n == 3.0f) c = mk3(aces1(c.x), aces1(c.y), aces1(c.z));
-    else if (n == 4.0f) c = pbr_neutral(c);
-    c = c * S.post[1] + S.post[2];
-    c = (c - mk3(0.5f)) * S.post[4] + mk3(0.5f);
-    float l = dot(c, mk3(0.2126f, 0.7152f, 0.0722f));
-    c = mix3(mk3(l), c, S.post[3]);
-    return clamp3(c, 0.0f, 1.0f);
-}
 __global__ void __launch_bounds__(256) present_kernel(const DeviceScene *scene, const float4 *accum, uchar4 *out) {
     const DeviceScene &S = *scene;
     uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u), y = blockIdx.y * 8u + (threadIdx.x >> 5);
@@ -77,6 +45,46 @@ __global__ void __launch_bounds__(256) present_kernel(const DeviceScene *scene, 
 }
 
 
+// typed_soa_validation_kernel (shaders/Shaders.metal:5106-5154): hash-seeded
+// points in the voxel bounds (plus the origin, both corners and the centre);
+// the lowered program's distance and gradient against the interpreter's.
+// counts: distance failures, gradient failures, max distance error bits, max
+// gradient error bits.
+__device__ __forceinline__ uint32_t validation_hash(uint32_t v) {   // lowbias32 (C. Wellons), as :4992-4999
+    v ^= v >> 16; v *= 0x7feb352du;
+    v ^= v >> 15; v *= 0x846ca68bu;
+    v ^= v >> 16;
+    return v;
+}
+static __global__ void __launch_bounds__(256) typed_soa_validation_kernel(const DeviceScene *scene, float3 bmin, float3 bmax,
+                                                                          uint32_t n, unsigned int *counts) {
+    const DeviceScene &S = *scene;
+    uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= n) return;
+    float3 u = mk3(float(validation_hash(gid * 3u + 0x9e3779b9u)), float(validation_hash(gid * 3u + 0x243f6a88u)),
+                   float(validation_hash(gid * 3u + 0xb7e15162u))) * (1.0f / 4294967295.0f);
+    float3 p = mk3(mixf(bmin.x, bmax.x, u.x), mixf(bmin.y, bmax.y, u.y), mixf(bmin.z, bmax.z, u.z));
+    if (gid == 0u) p = mk3(0.0f);
+    if (gid == 1u) p = bmin;
+    if (gid == 2u) p = bmax;
+    if (gid == 3u) p = (bmin + bmax) * 0.5f;
+    const float ref = program_distance(p, S, false).d, direct = soa_distance(p, S);
+    const float derr = fabsf(ref - direct);
+    if (!isfinite(ref) || !isfinite(direct) || derr > 2.0e-5f * (1.0f + fabsf(ref))) atomicAdd(counts + 0, 1u);
+    atomicMax(counts + 2, __float_as_uint(isfinite(derr) ? derr : 3.0e38f));
+    float3 rg = program_gradient(p, S, nullptr), dg;
+    soa_surface(p, S, dg);
+    const float gerr = fmaxf(fabsf(rg.x - dg.x), fmaxf(fabsf(rg.y - dg.y), fabsf(rg.z - dg.z)));
+    if (!finite3(rg) || !finite3(dg) || !(gerr <= 1.0e-4f)) atomicAdd(counts + 1, 1u);
+    atomicMax(counts + 3, __float_as_uint(isfinite(gerr) ? gerr : 3.0e38f));
+}
+cudaError_t launch_typed_soa_validation(const DeviceScene *scene, const float bmin[3], const float bmax[3], uint32_t n,
+                                        unsigned int *counts, cudaStream_t st) {
+    typed_soa_validation_kernel<<<(n + 255u) / 256u, 256, 0, st>>>(scene, make_float3(bmin[0], bmin[1], bmin[2]),
+                                                                    make_float3(bmax[0], bmax[1], bmax[2]), n, counts);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out, cudaStream_t st) {
     dim3 grid((W + 31u) / 32u, (H + 7u) / 8u);
     present_kernel<<<grid, 256, 0, st>>>(scene, accum, out);
@@ -89,6 +97,7 @@ cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, con
     cudaError_t launch_focus_k##n(DeviceScene *, cudaStream_t);                                                              \
     cudaError_t launch_sample_distance_k##n(const DeviceScene *, const float4 *, float4 *, float *, size_t, cudaStream_t);       \
     cudaError_t launch_label_k##n(const DeviceScene *, float4 *, size_t, cudaStream_t);                                      \
+    cudaError_t launch_diagnostic_k##n(const DeviceScene *, uint32_t, uint32_t, uint32_t, float, uchar4 *, cudaStream_t);     \
     cudaError_t launch_skip_primary_k##n(const DeviceScene *, uint32_t, uint32_t, const SkipArgs &, FptCudaPrimaryHit *,     \
                                          cudaStream_t);
 FPT_DECLARE_KIND(0)
@@ -117,6 +126,14 @@ cudaError_t launch_focus(uint32_t kind, DeviceScene *scene, cudaStream_t st) { F
 cudaError_t launch_sample_distance(uint32_t kind, const DeviceScene *scene, const float4 *pts, float4 *out, float *grads, size_t n,
                                    cudaStream_t st) {
     FPT_DISPATCH(kind, launch_sample_distance_k, scene, pts, out, grads, n, st)
+}
+cudaError_t launch_diagnostic(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, uint32_t mode, float max_distance,
+                              uchar4 *out, cudaStream_t st) {
+    FPT_DISPATCH(kind, launch_diagnostic_k, scene, W, H, mode, max_distance, out, st)
+}
+cudaError_t launch_diag_final(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out, cudaStream_t st) {
+    diag_final_kernel<<<(W * H + 255u) / 256u, 256, 0, st>>>(scene, accum, out);
+    return cudaGetLastError();
 }
 cudaError_t launch_label(uint32_t kind, const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t st) {
     FPT_DISPATCH(kind, launch_label_k, scene, pts, n, st)

@@ -7,6 +7,7 @@
 
 #include "fpt_march.cuh"
 #include "fpt_kernels.h"
+#include "diag.cuh"
 #include "skip.cuh"
 #include "wavefront.cuh"
 

@@ -122,6 +122,12 @@ cudaError_t FPT_CAT(launch_sample_distance_k, FPT_KIND)(const DeviceScene *scene
     sample_distance_kernel<FPT_KIND><<<blocks, 256, 0, st>>>(scene, pts, out, grads, n);
     return cudaGetLastError();
 }
+cudaError_t FPT_CAT(launch_diagnostic_k, FPT_KIND)(const DeviceScene *scene, uint32_t W, uint32_t H, uint32_t mode, float max_distance,
+                                                    uchar4 *out, cudaStream_t st) {
+    dim3 grid((W + 15u) / 16u, (H + 7u) / 8u);
+    diagnostic_kernel<FPT_KIND><<<grid, 128, 0, st>>>(scene, mode, max_distance, 0u, 0u, out);
+    return cudaGetLastError();
+}
 cudaError_t FPT_CAT(launch_label_k, FPT_KIND)(const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t st) {
     label_kernel<FPT_KIND><<<unsigned((n + 255) / 256), 256, 0, st>>>(scene, pts, n);
     return cudaGetLastError();

@@ -316,6 +316,68 @@ def mandelbulb_deep_zoom(eye, target, width: int = 64, height: int = 48, fov_deg
     return cfg, ext
 
 
+def flat_union_program(seed: int = 0, spheres: int = 6, boxes: int = 5, planes: int = 1, width: int = 160,
+                       height: int = 120) -> ffi.FptRenderConfig:
+    """A typed program that is a flat union of translated spheres, boxes and planes, together with its typed-SoA
+    lowering (sdf_typed_soa: each primitive's accumulated translation, sizes and source instruction), the form
+    the reference's scene loader produces for such programs.  Voxel bounds frame the validation samples."""
+    rng = np.random.default_rng(seed)
+    cfg = ffi.default_config()
+    cfg.width, cfg.height = width, height
+    cfg.sdf_id = ffi.SDF_PROGRAM
+    soa = cfg.sdf_typed_soa
+    prog, acc = [], np.zeros(3)
+
+    def move(to):
+        nonlocal acc
+        delta = np.asarray(to, np.float64) - acc
+        prog.append((ffi.OP_TRANSLATE, 0, (*delta, 0.0)))
+        acc = acc + delta
+        return acc.astype(np.float32)
+
+    kinds = ["s"] * spheres + ["b"] * boxes + ["p"] * planes
+    rng.shuffle(kinds)
+    for kind in kinds:
+        if kind == "p":
+            c = move((0.0, float(rng.uniform(-1.2, -0.8)), 0.0))
+            normal = np.array([rng.uniform(-0.1, 0.1), 1.0, rng.uniform(-0.1, 0.1)], np.float32)
+            offset = float(rng.uniform(-0.05, 0.05))
+            src = len(prog)
+            prog.append((ffi.OP_PLANE, 0, (*normal, offset)))
+            i = soa.plane_count
+            soa.plane_x[i], soa.plane_y[i], soa.plane_z[i] = (float(v) for v in normal)
+            soa.plane_center_x[i], soa.plane_center_y[i], soa.plane_center_z[i] = (float(v) for v in c)
+            soa.plane_offset[i], soa.plane_source[i] = offset, src
+            soa.plane_count += 1
+            continue
+        c = move(rng.uniform(-1.5, 1.5, 3) * np.array([1.0, 0.6, 1.0]))
+        src = len(prog)
+        if kind == "s":
+            r = float(rng.uniform(0.2, 0.5))
+            prog.append((ffi.OP_SPHERE, 0, (r, 0.0, 0.0, 0.0)))
+            i = soa.sphere_count
+            soa.sphere_x[i], soa.sphere_y[i], soa.sphere_z[i] = (float(v) for v in c)
+            soa.sphere_radius[i], soa.sphere_source[i] = r, src
+            soa.sphere_count += 1
+        else:
+            h = rng.uniform(0.15, 0.45, 3).astype(np.float32)
+            prog.append((ffi.OP_BOX, 0, (*h, 0.0)))
+            i = soa.box_count
+            soa.box_x[i], soa.box_y[i], soa.box_z[i] = (float(v) for v in c)
+            soa.box_half_x[i], soa.box_half_y[i], soa.box_half_z[i] = (float(v) for v in h)
+            soa.box_source[i] = src
+            soa.box_count += 1
+    for i, (op, flags, d) in enumerate(prog):
+        cfg.sdf_program[i].opcode = op
+        cfg.sdf_program[i].flags = flags
+        cfg.sdf_program[i].data[:] = [float(v) for v in d]
+    cfg.sdf_program_count = len(prog)
+    cfg.voxel_bounds_min[:] = [-2.0, -2.0, -2.0]
+    cfg.voxel_bounds_max[:] = [2.0, 2.0, 2.0]
+    cfg.camera_position[:] = [0.0, 0.6, -5.0]
+    return cfg
+
+
 def batch_scene(k: int, spp: int = 4, bounces: int = 3) -> SceneBundle:
     """Scene k of the batched workload, drawn from a PCG64 stream seeded by k: a Mandelbulb (power
     U[2, 12]), a Mandelbox (scale U[-2.5, -1.5]) or a 2:1 Mandelbulb / Menger hybrid; iterations U{4..16};

@@ -59,3 +59,41 @@ def test_batch_scene_generator_is_seeded():
         if x.ext.formula == ffi.FORMULA_MANDELBOX:
             assert -2.5 <= x.ext.box_scale <= -1.5
     assert kinds == {ffi.FORMULA_MANDELBULB, ffi.FORMULA_MANDELBOX, ffi.FORMULA_BULB_MENGER_HYBRID}
+
+
+def test_flat_union_lowering_matches_program():
+    """The typed-SoA arrays of scenes.flat_union_program give the program's distance (numpy restatement of both)."""
+    import numpy as np
+    from fractalpathtracer_gb300 import ffi, scenes
+    cfg = scenes.flat_union_program(3)
+    pts = np.random.default_rng(0).uniform(-2, 2, (2000, 3))
+    # interpreter semantics: accumulated translations, union of primitives
+    d_prog = np.full(len(pts), np.inf)
+    p = pts.copy()
+    for i in range(cfg.sdf_program_count):
+        op = cfg.sdf_program[i]
+        d = np.array(op.data[:])
+        if op.opcode == ffi.OP_TRANSLATE:
+            p = p - d[:3]
+        elif op.opcode == ffi.OP_SPHERE:
+            d_prog = np.minimum(d_prog, np.linalg.norm(p, axis=1) - d[0])
+        elif op.opcode == ffi.OP_BOX:
+            q = np.abs(p) - np.abs(d[:3])
+            d_prog = np.minimum(d_prog, np.minimum(q.max(1), 0) + np.linalg.norm(np.maximum(q, 0), axis=1))
+        elif op.opcode == ffi.OP_PLANE:
+            n = d[:3] / np.linalg.norm(d[:3])
+            d_prog = np.minimum(d_prog, p @ n + d[3])
+    t = cfg.sdf_typed_soa
+    d_soa = np.full(len(pts), np.inf)
+    for i in range(t.sphere_count):
+        d_soa = np.minimum(d_soa, np.linalg.norm(pts - [t.sphere_x[i], t.sphere_y[i], t.sphere_z[i]], axis=1) - t.sphere_radius[i])
+    for i in range(t.box_count):
+        q = np.abs(pts - [t.box_x[i], t.box_y[i], t.box_z[i]]) - [t.box_half_x[i], t.box_half_y[i], t.box_half_z[i]]
+        d_soa = np.minimum(d_soa, np.minimum(q.max(1), 0) + np.linalg.norm(np.maximum(q, 0), axis=1))
+    for i in range(t.plane_count):
+        n = np.array([t.plane_x[i], t.plane_y[i], t.plane_z[i]])
+        n /= np.linalg.norm(n)
+        c = np.array([t.plane_center_x[i], t.plane_center_y[i], t.plane_center_z[i]])
+        d_soa = np.minimum(d_soa, (pts - c) @ n + t.plane_offset[i])
+    assert t.sphere_count + t.box_count + t.plane_count == 12
+    assert np.abs(d_prog - d_soa).max() < 1e-5
