@@ -360,12 +360,13 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     PathLaunch pl{};
     pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height; pl.bounces = S.bounces;
     pl.accum = c.accum; pl.counters = c.counter; pl.march_blocks = c.march_blocks;
+    pl.march_schedule = c.march_schedule; pl.ilv_batch = c.ilv_batch;
     pl.profile = want_profile ? c.profile : nullptr;
     {
         // Wave scratch: path records and queues for up to wave_paths paths.
         const size_t tiles = size_t((S.width + 7u) / 8u) * ((S.height + 3u) / 4u) * 32u;
         size_t per_launch = tiles * std::min(step, sub_cap);
-        size_t cap = c.wave_paths ? c.wave_paths : (size_t(16) << 20);
+        size_t cap = c.wave_paths ? c.wave_paths : (size_t(64) << 20);   // one wave per 1080p 16 spp frame
         cap = std::min(cap, per_launch);
         pl.wave_paths = uint32_t(cap);
         if (!ensure_buffer(&c.wave, &c.cap_wave, cap * kWaveBytesPerPath, error, error_len)) return 1;
@@ -773,6 +774,21 @@ int fpt_test_typed_soa(const char *metallib_path, const struct FptRenderConfig *
         set_error(error, error_len, "typed-SoA validation failed: %u distance, %u gradient", counts[0], counts[1]);
         return 1;
     }
+    return 0;
+}
+
+int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks) {
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    ctx().wave_paths = wave_paths;
+    ctx().march_blocks = march_blocks;
+    return 0;
+}
+
+int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch) {
+    if (schedule > 1u || batch > 32u) return 1;
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    ctx().march_schedule = schedule;
+    ctx().ilv_batch = batch;
     return 0;
 }
 

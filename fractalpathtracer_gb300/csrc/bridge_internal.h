@@ -35,6 +35,8 @@ struct Context {
     // launch tuning (set by the autotuner entry point; 0 = defaults)
     uint32_t wave_paths = 0;   // paths per wave; 0 = min(all paths, 16M)
     int march_blocks = 0;
+    uint32_t march_schedule = 0;   // 0: lockstep, 1: orbit-interleaved (extension formulas)
+    uint32_t ilv_batch = 0;
 };
 
 Context &ctx();

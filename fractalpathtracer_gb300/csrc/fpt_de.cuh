@@ -391,51 +391,80 @@ template <class T> __device__ __forceinline__ void menger_step(T &x, T &y, T &z,
     dr = dr * T(s);
 }
 
+// The orbit loop as start / step / finish, so a march can run it one
+// iteration at a time (the orbit-interleaved march kernel) with the same
+// arithmetic as orbit_eval.
+template <class T> struct Orbit {
+    T x, y, z, dr, r;
+    T cx, cy, cz;   // the constant added after each step
+    int i;          // completed iterations
+    bool escaped;
+};
+
+template <class T> __device__ __forceinline__ void orbit_start(Orbit<T> &o, T px, T py, T pz) {
+    o.x = px; o.y = py; o.z = pz;
+    o.cx = px; o.cy = py; o.cz = pz;
+    o.dr = T(1.0f);
+    o.r = s_sqrt(px * px + py * py + pz * pz);
+    o.i = 0;
+    o.escaped = false;
+}
+
+// One iteration; returns false once the orbit is finished (escaped, not
+// finite -- the step is rolled back -- or max_iter iterations done).
 template <int KIND, class T>
-__device__ __forceinline__ OrbitResult<T> orbit_eval(const DeviceScene &S, T px, T py, T pz, int max_iter, float bailout) {
-    T x = px, y = py, z = pz;
-    T dr = T(1.0f);
-    T r = s_sqrt(x * x + y * y + z * z);
-    int iterations = 0;
-    bool escaped = false;
-    const int period = S.hybrid_period > 1u ? int(S.hybrid_period) : 3;
-    for (int i = 0; i < max_iter; ++i) {
-        T ox = x, oy = y, oz = z;
-        bool add_c = true;
-        if (KIND == KIND_BULB8) bulb8_step(x, y, z, dr, r);
-        else if (KIND == KIND_BULB) bulb_step(x, y, z, dr, r, S.power);
-        else if (KIND == KIND_BOX) box_step(x, y, z, dr, S);
-        else if (KIND == KIND_MENGER) { menger_step(x, y, z, dr, S.menger_scale); add_c = false; }
-        else {  // KIND_HYBRID
-            if (i % period == period - 1) { menger_step(x, y, z, dr, S.menger_scale); add_c = false; }
-            else if (S.power == 8.0f) bulb8_step(x, y, z, dr, r);
-            else bulb_step(x, y, z, dr, r, S.power);
-        }
-        if (add_c) { x = x + px; y = y + py; z = z + pz; }
-        r = s_sqrt(x * x + y * y + z * z);
-        iterations = i + 1;
-        if (!isfinite(s_val(r))) {
-            x = ox; y = oy; z = oz;
-            r = s_sqrt(x * x + y * y + z * z);
-            break;
-        }
-        if (s_val(r) > bailout) { escaped = true; break; }
+__device__ __forceinline__ bool orbit_step(Orbit<T> &o, const DeviceScene &S, int max_iter, float bailout) {
+    const T ox = o.x, oy = o.y, oz = o.z;
+    const int i = o.i;
+    bool add_c = true;
+    if (KIND == KIND_BULB8) bulb8_step(o.x, o.y, o.z, o.dr, o.r);
+    else if (KIND == KIND_BULB) bulb_step(o.x, o.y, o.z, o.dr, o.r, S.power);
+    else if (KIND == KIND_BOX) box_step(o.x, o.y, o.z, o.dr, S);
+    else if (KIND == KIND_MENGER) { menger_step(o.x, o.y, o.z, o.dr, S.menger_scale); add_c = false; }
+    else {  // KIND_HYBRID
+        const int period = S.hybrid_period > 1u ? int(S.hybrid_period) : 3;
+        if (i % period == period - 1) { menger_step(o.x, o.y, o.z, o.dr, S.menger_scale); add_c = false; }
+        else if (S.power == 8.0f) bulb8_step(o.x, o.y, o.z, o.dr, o.r);
+        else bulb_step(o.x, o.y, o.z, o.dr, o.r, S.power);
     }
+    if (add_c) { o.x = o.x + o.cx; o.y = o.y + o.cy; o.z = o.z + o.cz; }
+    o.r = s_sqrt(o.x * o.x + o.y * o.y + o.z * o.z);
+    o.i = i + 1;
+    if (!isfinite(s_val(o.r))) {
+        o.x = ox; o.y = oy; o.z = oz;
+        o.r = s_sqrt(o.x * o.x + o.y * o.y + o.z * o.z);
+        return false;
+    }
+    if (s_val(o.r) > bailout) { o.escaped = true; return false; }
+    return o.i < max_iter;
+}
+
+template <int KIND, class T> __device__ __forceinline__ OrbitResult<T> orbit_finish(const Orbit<T> &ob) {
     OrbitResult<T> o;
-    o.r = r; o.dr = dr; o.iterations = iterations; o.escaped = escaped;
+    o.r = ob.r; o.dr = ob.dr; o.iterations = ob.i; o.escaped = ob.escaped;
     if (KIND == KIND_MENGER) {
-        T qx = s_abs(x) - T(1.0f), qy = s_abs(y) - T(1.0f), qz = s_abs(z) - T(1.0f);
+        T qx = s_abs(ob.x) - T(1.0f), qy = s_abs(ob.y) - T(1.0f), qz = s_abs(ob.z) - T(1.0f);
         T mx = s_max(qx, T(0.0f)), my = s_max(qy, T(0.0f)), mz = s_max(qz, T(0.0f));
         T outside = s_sqrt(mx * mx + my * my + mz * mz);
-        o.d = (outside + s_min(s_max(qx, s_max(qy, qz)), T(0.0f))) / dr;
-    } else if (!(s_val(dr) > 0.0f)) {
-        o.d = r;
+        o.d = (outside + s_min(s_max(qx, s_max(qy, qz)), T(0.0f))) / ob.dr;
+    } else if (!(s_val(ob.dr) > 0.0f)) {
+        o.d = ob.r;
     } else if (KIND == KIND_BOX) {
-        o.d = r / dr;
+        o.d = ob.r / ob.dr;
     } else {
-        o.d = s_val(r) > 1.0f ? T(0.5f) * r * s_log(r) / dr : T(0.0f);
+        o.d = s_val(ob.r) > 1.0f ? T(0.5f) * ob.r * s_log(ob.r) / ob.dr : T(0.0f);
     }
     return o;
+}
+
+template <int KIND, class T>
+__device__ __forceinline__ OrbitResult<T> orbit_eval(const DeviceScene &S, T px, T py, T pz, int max_iter, float bailout) {
+    Orbit<T> o;
+    orbit_start(o, px, py, pz);
+    if (max_iter > 0)
+        while (orbit_step<KIND>(o, S, max_iter, bailout)) {
+        }
+    return orbit_finish<KIND>(o);
 }
 
 __device__ __forceinline__ int ext_iterations(const DeviceScene &S) {
@@ -813,6 +842,35 @@ __device__ __forceinline__ Eval ext_eval(const DeviceScene &S, float3 p) {
         if (plane < e.d) { e.d = plane; e.id = 1; }
     }
     return e;
+}
+
+// scene_eval<KIND>(S, p, EV_MAP).d of an extension formula in two halves
+// around its orbit (ext_field, mandel_finish, ground plane, render[6]).
+template <int KIND> __device__ __forceinline__ int ext_eval_begin(const DeviceScene &S, float3 p, Orbit<float> &o) {
+    if (S.sdf_id == FPT_SDF_MANDELBULBER) {
+        float x = p.x, y = p.y, z = p.z;
+        const float ws = fmaxf(S.set_values[0], 1.0f);
+        global_point(S, x, y, z);
+        orbit_start(o, x / ws, z / ws, y / ws);
+    } else {
+        orbit_start(o, p.x, p.y, p.z);
+    }
+    return ext_iterations(S);
+}
+template <int KIND> __device__ __forceinline__ float ext_eval_end(const DeviceScene &S, float3 p, const Orbit<float> &ob) {
+    OrbitResult<float> o = orbit_finish<KIND>(ob);
+    float d;
+    if (S.sdf_id == FPT_SDF_MANDELBULBER) {
+        o.d = o.d * fmaxf(S.set_values[0], 1.0f);
+        d = mandel_finish(S, p, Field4{o.d, o.r, o.dr, o.escaped ? -float(o.iterations) : float(o.iterations)}).d;
+    } else {
+        d = o.d;
+    }
+    if (S.ground_plane) {
+        const float plane = p.y - S.plane_height;
+        if (plane < d) d = plane;
+    }
+    return mixf(d, d / 2.0f, S.render[6]);
 }
 
 // One evaluation of the scene at p.  KIND selects a specialised estimator;

@@ -85,13 +85,16 @@ def declare(L: C.CDLL) -> None:
     L.fpt_cuda_mlp_gradients.argtypes = [C.c_uint64, fp, C.c_size_t, C.c_float, fp, C.c_size_t, fp] + err
     L.fpt_cuda_skip_stats.argtypes = [P(FptCudaSkipStats)]
     L.fpt_cuda_render_stats.argtypes = [P(FptCudaRenderStats)]
+    L.fpt_cuda_set_launch_shape.argtypes = [C.c_uint32, C.c_int32]
+    L.fpt_cuda_set_march_schedule.argtypes = [C.c_uint32, C.c_uint32]
     L.fpt_cuda_render_batch.argtypes = [cfg, ext, C.c_size_t, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_size_t,
                                         P(FptCudaBatchStats)] + err
     L.fpt_cuda_autotune_batch.argtypes = [cfg, ext, C.c_size_t, C.c_uint32, P(FptCudaTuneResult)] + err
     for name in ("fpt_cuda_voxel_build", "fpt_cuda_voxel_read", "fpt_cuda_dda_sequence", "fpt_cuda_voxel_render",
                  "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
                  "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
-                 "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch"):
+                 "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch", "fpt_cuda_set_launch_shape",
+                 "fpt_cuda_set_march_schedule"):
         getattr(L, name).restype = C.c_int
 
 
@@ -298,3 +301,15 @@ def autotune_batch(bundles, rounds=3) -> dict:
     _check(lib().fpt_cuda_autotune_batch(cfgs, exts, len(bundles), rounds, C.byref(r), e, len(e)), e)
     tried = [{k: getattr(r.tried[i], k) for k, _ in FptCudaTuneCandidate._fields_ if k != "_pad"} for i in range(r.candidates)]
     return {"chosen": r.chosen, "rounds": r.rounds, "workload_key": r.workload_key, "tried": tried}
+
+
+def set_launch_shape(wave_paths: int = 0, march_blocks: int = 0) -> None:
+    from .native import lib
+    lib().fpt_cuda_set_launch_shape(wave_paths, march_blocks)
+
+
+def set_march_schedule(schedule: int = 0, batch: int = 0) -> None:
+    """0: lockstep march (default), 1: orbit-interleaved march for the extension formulas."""
+    from .native import lib
+    if lib().fpt_cuda_set_march_schedule(schedule, batch) != 0:
+        raise ValueError("schedule must be 0 or 1 and batch 0..32")
