@@ -19,6 +19,8 @@ from __future__ import annotations
 
 import argparse
 import json
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -163,7 +165,6 @@ def main():
         return
 
     import ctypes
-    import numpy as np
     import torch
     torch.cuda.set_device(local)
     if world > 1:
@@ -312,6 +313,8 @@ def main():
                                         "peak": peaks.get("bf16_tflops", 1900.0), "unit": "TFLOP/s",
                                         "frac": tflops / peaks.get("bf16_tflops", 1900.0),
                                         "peak_source": "MEASURED_PEAKS.json bf16 burst" if peaks else "fallback"}
+    if rank == 0:
+        line["other_configs"] = other_configs(native, nx, scenes, measured_peaks())
     if rank == 0 and args.cpu_baseline:
         try:
             import oracle
@@ -332,6 +335,42 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def other_configs(native, nx, scenes, peaks):
+    """Device-timed lines for the other workloads of the path (not the headline): 320x240 power-8 Mandelbulb
+    primary rays; Menger fold + ground plane path tracing at 1280x720 16 spp; the 1024^3 Mandelbox occupancy-brick
+    build and 1080p primary + shadow DDA (with its HBM roofline: 4 B brick-table read + 3 B occupancy / fp16
+    distance per visited cell, 32 B output per pixel)."""
+    med = lambda v: sorted(v)[len(v) // 2]
+    out = {}
+    cfg, ext = scenes.mandelbulb_primary(320, 240)
+    for _ in range(3):
+        native.trace_primary(cfg, ext)
+    ms = med([native.trace_primary(cfg, ext)[1] for _ in range(7)])
+    out["mandelbulb_primary_320x240"] = {"ms": ms, "Mrays_per_s": 320 * 240 / ms / 1e3}
+    b = scenes.menger_plane(1280, 720, 16)
+    for _ in range(2):
+        native.cuda_render(b.cfg, b.ext, linear=False)
+    ms = med([native.cuda_render(b.cfg, b.ext, linear=False)[2] for _ in range(3)])
+    out["menger_plane_1280x720_16spp"] = {"ms": ms, "Mpaths_per_s": 1280 * 720 * 16 / ms / 1e3}
+    cfg, ext = scenes.voxel_mandelbox(1024, 1920, 1080)
+    info = nx.voxel_build(cfg, ext, 8)
+    info = nx.voxel_build(cfg, ext, 8)
+    for _ in range(2):
+        nx.voxel_render(cfg, ext, image=False)
+    runs = [nx.voxel_render(cfg, ext, image=False) for _ in range(5)]
+    hits, _, ms = sorted(runs, key=lambda r: r[2])[2]
+    cells = int(hits["steps"].astype(np.int64).sum() + hits["shadow_steps"].astype(np.int64).sum())
+    nbytes = cells * 7 + hits.size * 32
+    gbs = nbytes / (ms / 1e3) / 1e9
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    out["mandelbox_voxel_1024"] = {
+        "build_ms": info["build_ms"], "active_bricks": info["active_bricks"], "memory_bytes": info["memory_bytes"],
+        "render_ms": ms, "Mrays_per_s": 2 * hits.size / ms / 1e3, "cells_visited": cells,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                     "work": "7 B per visited cell + 32 B per pixel"}}
+    return out
 
 
 def run_only(args):
