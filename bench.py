@@ -86,6 +86,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def reduce_over_ranks(vals, world, device):
+    """Element-wise maximum of per-rank timings over all ranks (the job time is the slowest replica's)."""
+    if world <= 1:
+        return list(vals)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(vals), device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_throughput(paths_per_rank, steps, world, max_seconds):
+    """Whole-job Mpaths/s: every rank renders `paths_per_rank` per step (replicas, weak scaling)."""
+    return paths_per_rank * steps * world / max_seconds / 1e6
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -212,11 +228,7 @@ def main():
         return times
 
     def reduce_max(vals):
-        if world > 1:
-            t = torch.tensor(vals, device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return t.tolist()
-        return vals
+        return reduce_over_ranks(vals, world, "cuda")
 
     paths = W * H * SPP
     # ---- plain march
@@ -251,10 +263,10 @@ def main():
     barrier()
     p_ms, p_e2e, s_ms, s_e2e, b_ms = reduce_max([sum(plain["ms"]), sum(plain_e2e), sum(skip["ms"]), sum(skip_e2e),
                                                  sum(box["ms"])])
-    plain_value = paths * args.steps * world / (p_ms / 1e3) / 1e6
-    plain_e2e_v = paths * args.steps * world / p_e2e / 1e6
-    value = paths * args.steps * world / (s_ms / 1e3) / 1e6
-    e2e = paths * args.steps * world / s_e2e / 1e6
+    plain_value = job_throughput(paths, args.steps, world, p_ms / 1e3)
+    plain_e2e_v = job_throughput(paths, args.steps, world, p_e2e)
+    value = job_throughput(paths, args.steps, world, s_ms / 1e3)
+    e2e = job_throughput(paths, args.steps, world, s_e2e)
     # ---- equal hit distance: primary rays of the same camera, plain vs skip march
     hp, _ = native.trace_primary(cfg, ext)
     hs, _ = native.trace_primary(cfg, skip_ext)
@@ -280,7 +292,7 @@ def main():
         "plain": {"value": plain_value, "e2e": plain_e2e_v, "ms_per_step": p_ms / args.steps,
                   "de_evals_per_s": plain["march_evals"] / (sum(plain["ms"]) / 1e3)},
         "skip_over_plain": value / plain_value,
-        "box_only": {"value": paths * args.steps * world / (b_ms / 1e3) / 1e6, "ms_per_step": b_ms / args.steps,
+        "box_only": {"value": job_throughput(paths, args.steps, world, b_ms / 1e3), "ms_per_step": b_ms / args.steps,
                      "march_evals": box["march_evals"] // args.steps,
                      "note": "surrogate's box clip without the network (FPT_CUDA_SURROGATE_BOX)"},
         "hit_equality": {"primary_rays": W * H, "hit_agreement": hit_agree,
