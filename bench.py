@@ -167,7 +167,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
-    ap.add_argument("--only", default="", choices=["", "plain", "box", "skip"],
+    ap.add_argument("--only", default="", choices=["", "plain", "box", "skip", "voxel"],
                     help="render only this march (profiling runs: no training unless skip, no JSON contract line)")
     ap.add_argument("--res", default=f"{W}x{H}", help="--only runs: image size WxH")
     ap.add_argument("--spp", type=int, default=SPP, help="--only runs: samples per pixel")
@@ -390,6 +390,14 @@ def run_only(args):
     from fractalpathtracer_gb300 import build, native, native_ext as nx, scenes
     build.build()
     w, h = (int(v) for v in args.res.lower().split("x"))
+    if args.only == "voxel":   # 1024^3 Mandelbox occupancy bricks, primary + shadow DDA
+        cfg, ext = scenes.voxel_mandelbox(1024, w, h)
+        info = nx.voxel_build(cfg, ext, 8)
+        for _ in range(args.warmup):
+            nx.voxel_render(cfg, ext, image=False)
+        ms = [nx.voxel_render(cfg, ext, image=False)[2] for _ in range(args.steps)]
+        print(json.dumps({"only": "voxel", "build_ms": info["build_ms"], "ms": ms}), flush=True)
+        return
     b = scenes.mandelbulb_path(w, h, args.spp, BOUNCES)
     cfg, ext = b.cfg, b.ext
     model = None
