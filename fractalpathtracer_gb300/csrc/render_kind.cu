@@ -86,7 +86,10 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
             const int cur = int(b & 1u);
             reset_counters_kernel<<<1, 32, 0, stream>>>(W.counters, cur ^ 1);
             ++launches;
-            if (skip_pass)
+            // Rays of later passes leave a surface (distance under the hand-over
+            // margin), so the skip pass would hand them straight back: it runs on
+            // the camera rays only, the box clip applies in every pass.
+            if (skip_pass && b == 0u)
                 timed(KC_SKIP, [&] {
                     skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, cur, *pl.skip);
                 });
