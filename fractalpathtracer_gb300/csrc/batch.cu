@@ -238,7 +238,9 @@ bool render_plan(const BatchPlan &P, int variant, uint32_t wave_req, float &ms, 
     // focus prepass of scenes without a focus distance (outside the graph)
     for (size_t k = 0; k < n; ++k)
         if (P.scenes[k].focus_distance <= 0.0f) focus_kernel<KIND_EXT><<<1, 32, 0, c.stream>>>(B.scenes + k);
-    if (!check(cudaMemsetAsync(B.tables + 2 * (n + 1), 0, sizeof(uint32_t), c.stream), "pass reset", error, error_len)) return false;
+    if (!check(cudaMemsetAsync(B.tables + 2 * (n + 1), 0, sizeof(uint32_t), c.stream), "pass reset", error, error_len) ||
+        !check(cudaMemsetAsync(c.counter, 0, 64, c.stream), "counter reset", error, error_len))
+        return false;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -259,6 +261,12 @@ bool render_plan(const BatchPlan &P, int variant, uint32_t wave_req, float &ms, 
         cudaEventRecord(e1, c.stream);
         good = good && check(cudaStreamSynchronize(c.stream), "batch render", error, error_len);
         if (good) cudaEventElapsedTime(&ms, e0, e1);
+        uint32_t guard = 0;
+        if (good && check(cudaMemcpy(&guard, c.counter + C_GUARD, sizeof(guard), cudaMemcpyDeviceToHost), "guard readback", error,
+                          error_len) && guard) {
+            set_error(error, error_len, "a persistent march loop exceeded its 10 s limit and stopped (batch render aborted)");
+            good = false;
+        }
     }
     if (exec) cudaGraphExecDestroy(exec);
     cudaEventDestroy(e0);

@@ -335,6 +335,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     if (!ensure_buffer((void **)&c.accum, &c.cap_accum, pixels * sizeof(float4), error, error_len)) return 1;
     if (!ensure_buffer((void **)&c.rgba, &c.cap_rgba, pixels * sizeof(uchar4), error, error_len)) return 1;
     if (!ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len)) return 1;
+    if (!check(cudaMemsetAsync(c.counter, 0, 64, c.stream), "counter reset", error, error_len)) return 1;
     bool want_profile = profile_out != nullptr || hydrated.sdf_profile != 0u;
     if (want_profile) {
         if (!ensure_buffer((void **)&c.profile, &c.cap_profile, 8 * sizeof(unsigned long long), error, error_len)) return 1;
@@ -360,7 +361,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     PathLaunch pl{};
     pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height; pl.bounces = S.bounces;
     pl.accum = c.accum; pl.counters = c.counter; pl.march_blocks = c.march_blocks;
-    pl.march_schedule = c.march_schedule; pl.ilv_batch = c.ilv_batch;
+    pl.march_schedule = c.march_schedule; pl.ilv_batch = c.ilv_batch; pl.refill_batch = c.refill_batch;
     pl.profile = want_profile ? c.profile : nullptr;
     {
         // Wave scratch: path records and queues for up to wave_paths paths.
@@ -407,6 +408,15 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     ++launches;
     cudaEventRecord(c.ev1, c.stream);
     if (!check(cudaStreamSynchronize(c.stream), "CUDA render", error, error_len)) return 1;
+    {
+        uint32_t guard = 0;
+        if (!check(cudaMemcpy(&guard, c.counter + 8, sizeof(guard), cudaMemcpyDeviceToHost), "guard readback", error, error_len))
+            return 1;
+        if (guard) {
+            set_error(error, error_len, "a persistent march loop exceeded its 10 s limit and stopped (render aborted)");
+            return 1;
+        }
+    }
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     if (elapsed_ms) *elapsed_ms = double(ms);
@@ -788,7 +798,8 @@ int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch) {
     if (schedule > 1u || batch > 32u) return 1;
     std::lock_guard<std::mutex> lock(ctx().mutex);
     ctx().march_schedule = schedule;
-    ctx().ilv_batch = batch;
+    if (schedule == 1u) ctx().ilv_batch = batch;
+    else ctx().refill_batch = batch;
     return 0;
 }
 

@@ -37,6 +37,7 @@ struct Context {
     int march_blocks = 0;
     uint32_t march_schedule = 0;   // 0: lockstep, 1: orbit-interleaved (extension formulas)
     uint32_t ilv_batch = 0;
+    uint32_t refill_batch = 0;
 };
 
 Context &ctx();

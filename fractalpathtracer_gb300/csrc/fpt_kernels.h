@@ -53,6 +53,7 @@ struct PathLaunch {
     uint64_t *launches;         // host counter of kernel launches, or null
     uint32_t march_schedule;    // 0: lockstep, 1: orbit-interleaved (extension formulas)
     uint32_t ilv_batch;         // interleaved: lanes that finish together (0: 16)
+    uint32_t refill_batch;      // lockstep: finished lanes finish and refill together in groups of this many
 };
 
 cudaError_t launch_pathtrace(const PathLaunch &pl, cudaStream_t stream);

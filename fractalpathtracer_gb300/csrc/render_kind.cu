@@ -33,6 +33,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     }
     const bool skip_pass = pl.skip && pl.skip->use_network;
     W.ilv_batch = pl.ilv_batch;
+    W.refill_batch = pl.refill_batch;
     // extension formulas can march with the orbit-interleaved kernel (schedule 1)
     constexpr bool kExt = KIND == KIND_BULB8 || KIND == KIND_BULB || KIND == KIND_BOX || KIND == KIND_MENGER || KIND == KIND_HYBRID;
     const bool interleaved = kExt && pl.march_schedule == 1u;

@@ -194,7 +194,10 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WavePara
     uint32_t job = 0;
     bool shadow = false;
     uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
+    uint32_t trips = 0;
+    const unsigned long long t0 = global_ns();
     while (true) {
+        if (loop_guard(trips, t0, W.counters)) break;
         // Refill idle lanes (one atomic per warp); rays that miss the box are
         // resolved at once and the lane draws again.
         for (int tries = 0; tries < 4; ++tries) {

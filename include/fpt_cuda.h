@@ -846,10 +846,12 @@ int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
  * depend on either. */
 int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks);
 
-/* March schedule of later single-scene renders of the extension formulas:
- * 0 lockstep (default; each distance evaluation runs to completion), 1
- * orbit-interleaved (one orbit iteration per warp trip; `batch` lanes, 1-32,
- * finish their evaluations together, 0 = 16).  Images agree within FP32
+/* March schedule of later single-scene renders:
+ * 0 lockstep (default; each distance evaluation runs to completion; lanes
+ * whose ray finished write it and take the next ray together once `batch` of
+ * them wait: 0 = 8, 1 = at once), 1 orbit-interleaved, extension formulas
+ * only (one orbit iteration per warp trip; `batch` lanes, 1-32, finish their
+ * evaluations together, 0 = 16).  Images agree within FP32
  * rounding; on the power-8 Mandelbulb at 1080p the interleaved march took
  * 48-60 ms against 36 ms for lockstep. */
 int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch);
