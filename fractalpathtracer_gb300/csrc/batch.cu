@@ -15,7 +15,8 @@
 //
 // Autotuner: the march kernel is instantiated with several launch shapes
 // (block size x register cap through __launch_bounds__); together with the
-// wavefront length (paths per wave) they form the candidates.  Candidates are
+// wavefront length (paths per wave) and the march's finish/refill group size
+// they form the candidates.  Candidates are
 // timed on the batch itself in interleaved rounds (median per candidate); a
 // candidate replaces the default only when it is faster by a margin, and the
 // choice is kept for the batch's workload key (the measured-selection
@@ -52,6 +53,7 @@ constexpr double kTuneMargin = 0.03;   // a candidate must beat the default by 3
 struct TuneChoice {
     int variant = 0;
     uint32_t wave_paths = 0;   // 0: all paths of a pass in one wave (capped at 16M)
+    uint32_t refill = 0;       // finish/refill group of the march (0: the kernel's default)
 };
 
 std::map<uint64_t, TuneChoice> &tuned() {
@@ -157,7 +159,7 @@ uint32_t wave_for(const BatchPlan &P, uint32_t requested) {
 
 // Launches one pass of the batch on `st` (captured into the graph).  Returns
 // the number of kernel launches.
-uint32_t launch_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_paths, cudaStream_t st) {
+uint32_t launch_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_paths, uint32_t refill, cudaStream_t st) {
     Context &c = ctx();
     BatchState &B = bstate();
     const size_t n = P.scenes.size();
@@ -173,6 +175,7 @@ uint32_t launch_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_pa
     W.counters = c.counter;
     W.profile = nullptr;
     W.box_on = 0;
+    W.refill_batch = refill;
     const uint32_t cap = wave_paths;
     char *base = static_cast<char *>(c.wave);
     W.paths = reinterpret_cast<PathRec *>(base);
@@ -214,12 +217,13 @@ uint32_t launch_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_pa
 }
 
 // Captures one pass into a graph.
-bool capture_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_paths, cudaGraphExec_t &exec, uint32_t &launches,
+bool capture_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_paths, uint32_t refill, cudaGraphExec_t &exec,
+                  uint32_t &launches,
                   char *error, size_t error_len) {
     Context &c = ctx();
     cudaGraph_t graph = nullptr;
     if (!check(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal), "graph capture", error, error_len)) return false;
-    launches = launch_pass(P, V, wave_paths, c.stream);
+    launches = launch_pass(P, V, wave_paths, refill, c.stream);
     cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
     if (!check(e, "graph capture", error, error_len)) return false;
     e = cudaGraphInstantiate(&exec, graph, 0);
@@ -228,11 +232,12 @@ bool capture_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_paths
 }
 
 // Renders all spp passes with one graph; returns the device time of the replays.
-bool render_plan(const BatchPlan &P, int variant, uint32_t wave_req, float &ms, uint32_t &launches_per_pass, double &build_ms,
+bool render_plan(const BatchPlan &P, const TuneChoice &choice, float &ms, uint32_t &launches_per_pass, double &build_ms,
                  char *error, size_t error_len) {
     Context &c = ctx();
     BatchState &B = bstate();
-    const uint32_t wave = wave_for(P, wave_req);
+    const int variant = choice.variant;
+    const uint32_t wave = wave_for(P, choice.wave_paths);
     if (!upload_plan(P, wave, error, error_len)) return false;
     const size_t n = P.scenes.size();
     // focus prepass of scenes without a focus distance (outside the graph)
@@ -246,7 +251,7 @@ bool render_plan(const BatchPlan &P, int variant, uint32_t wave_req, float &ms, 
     cudaEventCreate(&e1);
     cudaEventRecord(e0, c.stream);
     cudaGraphExec_t exec = nullptr;
-    const bool ok = capture_pass(P, kVariants[variant], wave, exec, launches_per_pass, error, error_len);
+    const bool ok = capture_pass(P, kVariants[variant], wave, choice.refill, exec, launches_per_pass, error, error_len);
     cudaEventRecord(e1, c.stream);
     float bms = 0.0f;
     if (ok) {
@@ -298,7 +303,7 @@ int fpt_cuda_render_batch(const struct FptRenderConfig *configs, const struct Fp
     float ms = 0.0f;
     uint32_t launches = 0;
     double build_ms = 0.0;
-    if (!render_plan(P, choice.variant, choice.wave_paths, ms, launches, build_ms, error, error_len)) return 1;
+    if (!render_plan(P, choice, ms, launches, build_ms, error, error_len)) return 1;
     Context &c = ctx();
     BatchState &B = bstate();
     if (linear_output &&
@@ -327,6 +332,7 @@ int fpt_cuda_render_batch(const struct FptRenderConfig *configs, const struct Fp
         stats->block_size = uint32_t(V.block);
         stats->registers = uint32_t(fa.numRegs);
         stats->wave_paths = wave_for(P, choice.wave_paths);
+        stats->refill = choice.refill;
         stats->tuned = was_tuned ? 1u : 0u;
         stats->workload_key = P.key;
     }
@@ -341,19 +347,20 @@ int fpt_cuda_autotune_batch(const struct FptRenderConfig *configs, const struct 
     BatchPlan P;
     if (!make_plan(configs, exts, count, P, error, error_len)) return 1;
     rounds = std::max<uint32_t>(std::min<uint32_t>(rounds, 15), 1);
-    struct Cand { int variant; uint32_t wave; std::vector<float> ms; };
+    struct Cand { TuneChoice choice; std::vector<float> ms; };
     std::vector<Cand> cands;
     const uint32_t waves[3] = {0u, 1u << 20, 4u << 20};
-    for (int v = 0; v < kVariantCount; ++v) cands.push_back({v, 0u, {}});
+    for (int v = 0; v < kVariantCount; ++v) cands.push_back({TuneChoice{v, 0u, 0u}, {}});
     for (int w = 1; w < 3; ++w)
-        if (waves[w] < P.work) cands.push_back({0, waves[w], {}});
+        if (waves[w] < P.work) cands.push_back({TuneChoice{0, waves[w], 0u}, {}});
+    for (uint32_t refill : {1u, 4u, 16u}) cands.push_back({TuneChoice{0, 0u, refill}, {}});
     // warm-up once per candidate, then interleaved timed rounds
     for (int r = -1; r < int(rounds); ++r)
         for (auto &cd : cands) {
             float ms = 0.0f;
             uint32_t launches = 0;
             double build_ms = 0.0;
-            if (!render_plan(P, cd.variant, cd.wave, ms, launches, build_ms, error, error_len)) return 1;
+            if (!render_plan(P, cd.choice, ms, launches, build_ms, error, error_len)) return 1;
             if (r >= 0) cd.ms.push_back(ms);
         }
     auto median = [](std::vector<float> v) {
@@ -367,19 +374,20 @@ int fpt_cuda_autotune_batch(const struct FptRenderConfig *configs, const struct 
         const double m = median(cands[i].ms);
         if (m < best_ms && m < base * (1.0 - kTuneMargin)) { best_ms = m; best = i; }
     }
-    tuned()[P.key] = TuneChoice{cands[best].variant, cands[best].wave};
+    tuned()[P.key] = cands[best].choice;
     if (result) {
         result->candidates = uint32_t(std::min<size_t>(cands.size(), 16));
         result->chosen = uint32_t(best);
         result->rounds = rounds;
         result->workload_key = P.key;
         for (size_t i = 0; i < cands.size() && i < 16; ++i) {
-            const MarchVariant &V = kVariants[cands[i].variant];
+            const MarchVariant &V = kVariants[cands[i].choice.variant];
             cudaFuncAttributes fa{};
             cudaFuncGetAttributes(&fa, V.fn);
             result->tried[i].block_size = uint32_t(V.block);
             result->tried[i].registers = uint32_t(fa.numRegs);
-            result->tried[i].wave_paths = wave_for(P, cands[i].wave);
+            result->tried[i].wave_paths = wave_for(P, cands[i].choice.wave_paths);
+            result->tried[i].refill = cands[i].choice.refill;
             result->tried[i].median_ms = median(cands[i].ms);
         }
     }

@@ -45,11 +45,11 @@ class FptCudaBatchStats(C.Structure):
     _fields_ = [("elapsed_ms", C.c_double), ("build_ms", C.c_double), ("paths", C.c_uint64), ("scenes", C.c_uint32),
                 ("passes", C.c_uint32), ("graph_launches", C.c_uint32), ("kernel_launches_per_pass", C.c_uint32),
                 ("block_size", C.c_uint32), ("registers", C.c_uint32), ("wave_paths", C.c_uint32), ("tuned", C.c_uint32),
-                ("workload_key", C.c_uint64)]
+                ("workload_key", C.c_uint64), ("refill", C.c_uint32), ("_pad", C.c_uint32)]
 
 
 class FptCudaTuneCandidate(C.Structure):
-    _fields_ = [("block_size", C.c_uint32), ("registers", C.c_uint32), ("wave_paths", C.c_uint32), ("_pad", C.c_uint32),
+    _fields_ = [("block_size", C.c_uint32), ("registers", C.c_uint32), ("wave_paths", C.c_uint32), ("refill", C.c_uint32),
                 ("median_ms", C.c_double)]
 
 
@@ -290,7 +290,7 @@ def render_batch(bundles, linear=True, rgba=False):
         if img is not None:
             out_img.append(img[off * 4:(off + h * w) * 4].reshape(h, w, 4))
         off += h * w
-    return out_lin, out_img, {k: getattr(st, k) for k, _ in FptCudaBatchStats._fields_}
+    return out_lin, out_img, {k: getattr(st, k) for k, _ in FptCudaBatchStats._fields_ if k != "_pad"}
 
 
 def autotune_batch(bundles, rounds=3) -> dict:

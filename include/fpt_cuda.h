@@ -880,6 +880,8 @@ struct FptCudaBatchStats {
     uint32_t wave_paths;         /* paths per wave */
     uint32_t tuned;              /* 1 when the autotuner's choice was used */
     uint64_t workload_key;
+    uint32_t refill;             /* march finish/refill group (0: default 8) */
+    uint32_t _pad;
 };
 int fpt_cuda_render_batch(const struct FptRenderConfig *configs,
                           const struct FptCudaSceneExt *exts,
@@ -896,7 +898,7 @@ struct FptCudaTuneCandidate {
     uint32_t block_size;
     uint32_t registers;
     uint32_t wave_paths;
-    uint32_t _pad;
+    uint32_t refill;             /* march finish/refill group (0: default 8) */
     double median_ms;            /* median render time over the timed rounds */
 };
 struct FptCudaTuneResult {
