@@ -171,6 +171,8 @@ def main():
                     help="render only this march (profiling runs: no training unless skip, no JSON contract line)")
     ap.add_argument("--res", default=f"{W}x{H}", help="--only runs: image size WxH")
     ap.add_argument("--spp", type=int, default=SPP, help="--only runs: samples per pixel")
+    ap.add_argument("--engine", default="tcgen05", choices=["tcgen05", "mma_sync"],
+                    help="surrogate network engine of the skip arm")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
@@ -189,6 +191,8 @@ def main():
     from fractalpathtracer_gb300 import build, native, native_ext as nx, scenes
     build.build()
     native.lib()
+    engine = nx.NET_TCGEN05 if args.engine == "tcgen05" else nx.NET_MMA_SYNC
+    nx.set_network_engine(engine)
     b = scenes.mandelbulb_path(W, H, SPP, BOUNCES)
     cfg, ext = b.cfg, b.ext
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -253,6 +257,15 @@ def main():
     skip_stats = nx.skip_stats()
     skip_e2e = e2e_series(skip_ext, args.steps)
     barrier()
+    # ---- the same skip march with the network on the other engine (comparison only)
+    other = nx.NET_MMA_SYNC if engine == nx.NET_TCGEN05 else nx.NET_TCGEN05
+    nx.set_network_engine(other)
+    for _ in range(args.warmup):
+        native.cuda_render(cfg, skip_ext, linear=False)
+    barrier()
+    skip_other = series(skip_ext, args.steps)
+    nx.set_network_engine(engine)
+    barrier()
     # ---- the same march without the network (the model's box only)
     box_ext = ffi_copy(skip_ext)
     box_ext.surrogate = 2
@@ -261,8 +274,8 @@ def main():
     barrier()
     box = series(box_ext, args.steps)
     barrier()
-    p_ms, p_e2e, s_ms, s_e2e, b_ms = reduce_max([sum(plain["ms"]), sum(plain_e2e), sum(skip["ms"]), sum(skip_e2e),
-                                                 sum(box["ms"])])
+    p_ms, p_e2e, s_ms, s_e2e, b_ms, o_ms = reduce_max([sum(plain["ms"]), sum(plain_e2e), sum(skip["ms"]), sum(skip_e2e),
+                                                       sum(box["ms"]), sum(skip_other["ms"])])
     plain_value = job_throughput(paths, args.steps, world, p_ms / 1e3)
     plain_e2e_v = job_throughput(paths, args.steps, world, p_e2e)
     value = job_throughput(paths, args.steps, world, s_ms / 1e3)
@@ -275,7 +288,8 @@ def main():
     hit_agree = float(((hp["hit"] > 0) == (hs["hit"] > 0)).mean())
     nx.mlp_destroy(model)
     # ---- roofline of the dominant kernel (the march kernel), timed live over the timed region
-    dom = "march_kernel" if skip["march_ms"] >= skip["skip_ms"] else "skip_march_kernel"
+    skip_kernel = "skip_march_tc_kernel" if engine == nx.NET_TCGEN05 else "skip_march_kernel"
+    dom = "march_kernel" if skip["march_ms"] >= skip["skip_ms"] else skip_kernel
     march_launch_ms = skip["march_ms"] / max(skip["march_launches"], 1)
     evals_per_launch = skip["march_evals"] / max(skip["march_launches"], 1)
     achieved = evals_per_launch * DE_FP32_OPS / (march_launch_ms / 1e3) / 1e12
@@ -292,6 +306,10 @@ def main():
         "plain": {"value": plain_value, "e2e": plain_e2e_v, "ms_per_step": p_ms / args.steps,
                   "de_evals_per_s": plain["march_evals"] / (sum(plain["ms"]) / 1e3)},
         "skip_over_plain": value / plain_value,
+        "network_engine": args.engine,
+        "skip_other_engine": {"engine": "mma_sync" if engine == nx.NET_TCGEN05 else "tcgen05",
+                              "value": job_throughput(paths, args.steps, world, o_ms / 1e3),
+                              "ms_per_step": o_ms / args.steps, "skip_ms": skip_other["skip_ms"] / args.steps},
         "box_only": {"value": job_throughput(paths, args.steps, world, b_ms / 1e3), "ms_per_step": b_ms / args.steps,
                      "march_evals": box["march_evals"] // args.steps,
                      "note": "surrogate's box clip without the network (FPT_CUDA_SURROGATE_BOX)"},
@@ -321,7 +339,7 @@ def main():
         rows = skip_stats["forwards"] * 32   # per render (the statistics of the last render)
         tflops = rows * MLP_FLOP / (skip["skip_ms"] / args.steps / 1e3) / 1e12
         peaks = measured_peaks()
-        line["roofline_skip_kernel"] = {"bound": "tensor", "achieved": tflops,
+        line["roofline_skip_kernel"] = {"kernel": skip_kernel, "bound": "tensor", "achieved": tflops,
                                         "peak": peaks.get("bf16_tflops", 1900.0), "unit": "TFLOP/s",
                                         "frac": tflops / peaks.get("bf16_tflops", 1900.0),
                                         "peak_source": "MEASURED_PEAKS.json bf16 burst" if peaks else "fallback"}
@@ -389,6 +407,7 @@ def run_only(args):
     """One march variant at the bench workload, for profiler launch lists (small surrogate for skip/box)."""
     from fractalpathtracer_gb300 import build, native, native_ext as nx, scenes
     build.build()
+    nx.set_network_engine(nx.NET_TCGEN05 if args.engine == "tcgen05" else nx.NET_MMA_SYNC)
     w, h = (int(v) for v in args.res.lower().split("x"))
     if args.only == "voxel":   # 1024^3 Mandelbox occupancy bricks, primary + shadow DDA
         cfg, ext = scenes.voxel_mandelbox(1024, w, h)
@@ -410,7 +429,10 @@ def run_only(args):
     for _ in range(args.warmup):
         native.cuda_render(cfg, ext, linear=False)
     ms = [native.cuda_render(cfg, ext, linear=False)[2] for _ in range(args.steps)]
-    print(json.dumps({"only": args.only, "ms": ms, "stats": nx.render_stats()}), flush=True)
+    out = {"only": args.only, "engine": args.engine, "ms": ms, "stats": nx.render_stats()}
+    if args.only == "skip":
+        out["skip_stats"] = nx.skip_stats()
+    print(json.dumps(out), flush=True)
     if model is not None:
         nx.mlp_destroy(model)
 

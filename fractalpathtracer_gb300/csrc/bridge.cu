@@ -386,6 +386,8 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     KernelTimer timer;
     uint64_t launches = 0;
     pl.launches = &launches;
+    uint32_t grids[2] = {0, 0};
+    pl.grids = grids;
     if (want_profile) {
         if (!c.timer_events) {
             c.timer_capacity = 1024;
@@ -410,10 +412,11 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     if (!check(cudaStreamSynchronize(c.stream), "CUDA render", error, error_len)) return 1;
     {
         uint32_t guard = 0;
-        if (!check(cudaMemcpy(&guard, c.counter + 8, sizeof(guard), cudaMemcpyDeviceToHost), "guard readback", error, error_len))
+        if (!check(cudaMemcpy(&guard, c.counter + C_GUARD, sizeof(guard), cudaMemcpyDeviceToHost), "guard readback", error, error_len))
             return 1;
         if (guard) {
-            set_error(error, error_len, "a persistent march loop exceeded its 10 s limit and stopped (render aborted)");
+            set_error(error, error_len, (guard & 2u) ? "a surrogate network MMA did not complete within 1 s (render aborted)"
+                                                     : "a persistent march loop exceeded its 10 s limit and stopped (render aborted)");
             return 1;
         }
     }
@@ -425,6 +428,8 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         std::memset(&rs, 0, sizeof(rs));
         rs.kernel_launches = launches + (hydrated.focus_distance <= 0.0f ? 1u : 0u);
         rs.total_ms = ms;
+        rs.march_grid = grids[0];
+        rs.skip_grid = grids[1];
         double cat_ms[KC_COUNT] = {0.0, 0.0, 0.0};
         uint64_t cat_n[KC_COUNT] = {0, 0, 0};
         for (int i = 0; i < timer.n; ++i) {
@@ -539,12 +544,27 @@ int fpt_cuda_trace_primary(const struct FptRenderConfig *config, const struct Fp
             !surrogate_args(ext->surrogate_model, S, c.skip_stats, skip, error, error_len))
             return 1;
     }
+    if (S.surrogate) {
+        if (!ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len) ||
+            !check(cudaMemsetAsync(c.counter, 0, 64, c.stream), "counter reset", error, error_len))
+            return 1;
+        skip.guard = c.counter + C_GUARD;
+    }
     cudaEventRecord(c.ev0, c.stream);
     cudaError_t le = S.surrogate ? launch_skip_primary(S.kind, c.scene, S.width, S.height, skip, c.hits, c.stream)
                                  : launch_trace_primary(S.kind, c.scene, S.width, S.height, c.hits, c.stream);
     if (!check(le, "primary-ray launch", error, error_len)) return 1;
     cudaEventRecord(c.ev1, c.stream);
     if (!check(cudaStreamSynchronize(c.stream), "primary-ray trace", error, error_len)) return 1;
+    if (S.surrogate) {
+        uint32_t guard = 0;
+        if (!check(cudaMemcpy(&guard, c.counter + C_GUARD, sizeof(guard), cudaMemcpyDeviceToHost), "guard readback", error, error_len))
+            return 1;
+        if (guard) {
+            set_error(error, error_len, "a surrogate network MMA did not complete within 1 s (trace aborted)");
+            return 1;
+        }
+    }
     if (S.surrogate &&
         !check(cudaMemcpy(c.last_skip, c.skip_stats, sizeof(c.last_skip), cudaMemcpyDeviceToHost), "skip stats readback", error,
                error_len))
@@ -800,6 +820,13 @@ int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch) {
     ctx().march_schedule = schedule;
     if (schedule == 1u) ctx().ilv_batch = batch;
     else ctx().refill_batch = batch;
+    return 0;
+}
+
+int fpt_cuda_set_network_engine(uint32_t engine) {
+    if (engine > FPT_CUDA_NET_MMA_SYNC) return 1;
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    ctx().network_engine = engine;
     return 0;
 }
 

@@ -29,6 +29,7 @@
 #include "fpt_kernels.h"
 #include "fpt_math.cuh"
 #include "mlp.cuh"
+#include "mlp_tc.cuh"
 #include "skip.cuh"
 
 namespace fpt {
@@ -314,6 +315,25 @@ __global__ void __launch_bounds__(128) predict_kernel(Model M, const float4 *pts
         if (i < n) out[i] = o * M.label_scale;
     }
 }
+// The same prediction with the network on tcgen05: 128 points per CTA
+// iteration.  *fail_word gets bit 2 if an MMA did not complete.
+__global__ void __launch_bounds__(kTcRows) predict_tc_kernel(Model M, const float4 *pts, float *out, uint32_t n, uint32_t *fail_word) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    TcSmem &sm = *reinterpret_cast<TcSmem *>(smem_raw);
+    tc_setup(sm, M);
+    uint32_t phase = 0;
+    bool fail = false;
+    for (uint32_t base = blockIdx.x * uint32_t(kTcRows); base < n; base += gridDim.x * uint32_t(kTcRows)) {
+        const uint32_t i = base + threadIdx.x;
+        const float4 p = i < n ? pts[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float u[3] = {(p.x - M.center[0]) * M.inv_half[0], (p.y - M.center[1]) * M.inv_half[1], (p.z - M.center[2]) * M.inv_half[2]};
+        const float o = tc_forward(sm, phase, u, fail);
+        if (fail) break;   // the same in every thread
+        if (i < n) out[i] = o * M.label_scale;
+    }
+    tc_teardown(sm);
+    if (fail && threadIdx.x == 0) atomicOr(fail_word, 2u);
+}
 size_t forward_smem_bytes() { return ((sizeof(SmemWeights) + 127) & ~size_t(127)) + 4 * sizeof(WarpForward); }
 size_t train_smem_bytes() { return ((sizeof(SmemWeights) + 127) & ~size_t(127)) + kWarpsTrain * sizeof(WarpTrain); }
 
@@ -381,6 +401,7 @@ static void set_attributes() {
     if (done) return;
     cudaFuncSetAttribute(train_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(train_smem_bytes()));
     cudaFuncSetAttribute(predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(forward_smem_bytes()));
+    cudaFuncSetAttribute(predict_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc_smem_bytes()));
     done = true;
 }
 
@@ -434,6 +455,8 @@ bool surrogate_args(uint64_t model, const DeviceScene &S, unsigned long long *st
     A.safety = S.surrogate_safety > 0.0f ? S.surrogate_safety : 0.9f;
     A.max_iters = 64;
     A.use_network = S.surrogate == FPT_CUDA_SURROGATE_SKIP ? 1u : 0u;
+    A.engine = ctx().network_engine;
+    A.guard = nullptr;
     A.stats = stats;
     return true;
 }
@@ -616,12 +639,30 @@ int fpt_cuda_mlp_predict(uint64_t model, const float *points_xyzw, size_t n, flo
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     mlp::set_attributes();
-    const unsigned blocks = unsigned(std::min<size_t>((n + 127) / 128, size_t(sms) * 8));
-    mlp::predict_kernel<<<blocks, 128, mlp::forward_smem_bytes(), c.stream>>>(hm->view(), c.points, c.grads, uint32_t(n));
+    const bool tc = c.network_engine == FPT_CUDA_NET_TCGEN05;
+    if (tc && (!ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len) ||
+               !check(cudaMemsetAsync(c.counter, 0, 64, c.stream), "counter reset", error, error_len)))
+        return 1;
+    if (tc) {
+        const int per_sm = mlp::tc_blocks_per_sm(reinterpret_cast<const void *>(mlp::predict_tc_kernel));
+        const unsigned blocks = unsigned(std::min<size_t>((n + mlp::kTcRows - 1) / mlp::kTcRows, size_t(sms) * size_t(std::max(per_sm, 1))));
+        mlp::predict_tc_kernel<<<blocks, mlp::kTcRows, mlp::tc_smem_bytes(), c.stream>>>(hm->view(), c.points, c.grads, uint32_t(n),
+                                                                                          c.counter + C_GUARD);
+    } else {
+        const unsigned blocks = unsigned(std::min<size_t>((n + 127) / 128, size_t(sms) * 8));
+        mlp::predict_kernel<<<blocks, 128, mlp::forward_smem_bytes(), c.stream>>>(hm->view(), c.points, c.grads, uint32_t(n));
+    }
     if (!check(cudaGetLastError(), "prediction launch", error, error_len) ||
         !check(cudaMemcpyAsync(distances, c.grads, n * sizeof(float), cudaMemcpyDeviceToHost, c.stream), "prediction readback", error, error_len))
         return 1;
-    return check(cudaStreamSynchronize(c.stream), "prediction", error, error_len) ? 0 : 1;
+    if (!check(cudaStreamSynchronize(c.stream), "prediction", error, error_len)) return 1;
+    if (tc) {
+        uint32_t guard = 0;
+        if (!check(cudaMemcpy(&guard, c.counter + C_GUARD, sizeof(guard), cudaMemcpyDeviceToHost), "guard readback", error, error_len))
+            return 1;
+        if (guard) { set_error(error, error_len, "a surrogate network MMA did not complete within 1 s"); return 1; }
+    }
+    return 0;
 }
 
 int fpt_cuda_mlp_get_params(uint64_t model, float *params, size_t len, char *error, size_t error_len) {

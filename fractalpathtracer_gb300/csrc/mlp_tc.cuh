@@ -1,0 +1,215 @@
+// mlp_tc.cuh -- the surrogate's forward pass on the 5th-generation tensor
+// cores (tcgen05): 128 rows per CTA, one row per thread.
+//
+// Per layer, one thread issues the K/16 MMAs of a 128 x 64 x K product into
+// a 128 x 64 FP32 accumulator in tensor memory and commits them to an
+// mbarrier; every thread then reads its own row of the accumulator (TMEM
+// lane = thread), adds the bias, applies SiLU and writes the BF16 row into
+// the activation tile that the next layer's MMAs read.  The arithmetic is
+// that of mlp::forward32 (BF16 features, weights and activations, FP32
+// accumulation, the f16x2-tanh SiLU of inference, FP32 output layer); only
+// the order of the FP32 sums differs.
+#pragma once
+
+#include "mlp.cuh"
+#include "umma.cuh"
+
+namespace fpt {
+namespace mlp {
+
+constexpr int kTcRows = 128;           // M of every MMA; the CTA has one thread per row
+constexpr uint32_t kTcCols = 64;       // tensor-memory columns: one 128 x 64 FP32 accumulator
+constexpr uint32_t kCore = 128;        // bytes of one 8 x 8 BF16 core matrix
+// Activation tile [k chunk][row group][8 rows][8 bf16]: K-adjacent core
+// matrices lie 16 row groups apart, M-adjacent ones 128 bytes apart.
+constexpr uint32_t kActK = (kTcRows / 8) * kCore;   // 2048
+// Weight tile W[n][k] [k chunk][n group][8 rows][8 bf16].
+constexpr uint32_t kWK = (kHid / 8) * kCore;        // 1024
+constexpr uint32_t kTcIdesc = umma::idesc_bf16_f32(kTcRows, kHid);
+constexpr unsigned long long kMmaWaitNs = 1000000000ull;   // 1 s; a layer takes about a microsecond
+
+struct TcSmem {
+    alignas(1024) unsigned char act[kTcRows * kInPad * 2];   // layer-0 features (K = 112), then hidden rows (K = 64)
+    alignas(128) unsigned char w0[kHid * kInPad * 2];
+    alignas(128) unsigned char w[kHidden - 1][kHid * kHid * 2];
+    float b[kHidden][kHid];
+    float w4[kHid];
+    float b4;
+    uint32_t tmem;                                          // tensor-memory base of the accumulator
+    alignas(8) uint64_t bar;                                // MMA completion
+    // Slack after the tiles: the tensor core reads each tile through a
+    // descriptor, and this keeps those reads inside the CTA's shared memory
+    // whatever the descriptor strides.
+    unsigned char slack[4096];
+};
+inline size_t tc_smem_bytes() { return sizeof(TcSmem); }
+
+// Resident CTAs per SM of a kernel built on tc_forward, from its registers,
+// its shared memory, the thread and block limits and the 512 tensor-memory
+// columns.  (cudaOccupancyMaxActiveBlocksPerMultiprocessor answers 1 for
+// these kernels on GB300, where registers and shared memory allow 3.)
+inline int tc_blocks_per_sm(const void *kernel) {
+    cudaFuncAttributes fa{};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 1;
+    int regs_sm = 0, smem_sm = 0, smem_res = 0, threads_sm = 0, blocks_sm = 0;
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&smem_res, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    cudaDeviceGetAttribute(&blocks_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev);
+    const int regs_block = ((fa.numRegs * 32 + 255) / 256) * 256 * (kTcRows / 32);   // allocated per warp in units of 256
+    const int smem_block = int(tc_smem_bytes()) + int(fa.sharedSizeBytes) + smem_res;
+    int n = int(512u / kTcCols);
+    n = regs_block > 0 ? (regs_sm / regs_block < n ? regs_sm / regs_block : n) : n;
+    n = smem_sm / smem_block < n ? smem_sm / smem_block : n;
+    n = threads_sm / kTcRows < n ? threads_sm / kTcRows : n;
+    n = blocks_sm < n ? blocks_sm : n;
+    return n > 0 ? n : 1;
+}
+
+__device__ __forceinline__ uint32_t act_offset(int row, int kc) { return (uint32_t(kc) * (kTcRows / 8) + uint32_t(row >> 3)) * kCore + uint32_t(row & 7) * 16u; }
+__device__ __forceinline__ uint32_t w_core_offset(int n, int k) {
+    return (uint32_t(k >> 3) * (kHid / 8) + uint32_t(n >> 3)) * kCore + uint32_t(n & 7) * 16u + uint32_t(k & 7) * 2u;
+}
+
+// Weights into the core-matrix tiles, tensor memory and the mbarrier.  All
+// threads of the 128-thread CTA call it; it ends with a barrier.
+__device__ __forceinline__ void tc_setup(TcSmem &sm, const Model &M) {
+    for (int i = threadIdx.x; i < kHid * kInPad; i += blockDim.x) {
+        const int n = i / kInPad, k = i - n * kInPad;
+        *reinterpret_cast<__nv_bfloat16 *>(sm.w0 + w_core_offset(n, k)) = M.wbf[kW0 + i];
+    }
+    for (int l = 1; l < kHidden; ++l)
+        for (int i = threadIdx.x; i < kHid * kHid; i += blockDim.x) {
+            const int n = i / kHid, k = i - n * kHid;
+            *reinterpret_cast<__nv_bfloat16 *>(sm.w[l - 1] + w_core_offset(n, k)) = M.wbf[w_offset(l) + i];
+        }
+    for (int i = threadIdx.x; i < kHidden * kHid; i += blockDim.x) sm.b[i / kHid][i % kHid] = M.params[b_offset(i / kHid) + i % kHid];
+    for (int i = threadIdx.x; i < kHid; i += blockDim.x) sm.w4[i] = __bfloat162float(M.wbf[kW4 + i]);
+    if (threadIdx.x == 0) {
+        sm.b4 = M.params[kB4];
+        umma::mbar_init(&sm.bar, 1u);
+    }
+    if (threadIdx.x < 32) {
+        __syncwarp();
+        umma::tmem_alloc(&sm.tmem, kTcCols);
+        umma::tmem_relinquish();
+    }
+    umma::fence_smem_to_async();   // the weight tiles are read by the tensor core
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+}
+
+// Frees the tensor memory; all threads call it (after their last forward).
+__device__ __forceinline__ void tc_teardown(TcSmem &sm) {
+    umma::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        __syncwarp();
+        umma::fence_after_sync();
+        umma::tmem_dealloc(sm.tmem, kTcCols);
+    }
+}
+
+// The features of mlp::features, as 56 packed BF16 pairs (element 2p in the
+// low half of pair p).
+__device__ __forceinline__ void feature_pairs(const float u[3], uint32_t f[kInPad / 2]) {
+#pragma unroll
+    for (int p = 0; p < kInPad / 2; ++p) f[p] = 0u;
+    auto put = [&](int e, float v) {
+        const uint32_t b = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v)));
+        f[e >> 1] |= (e & 1) ? (b << 16) : b;
+    };
+    put(0, u[0]);
+    put(1, u[1]);
+    put(2, u[2]);
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+        const float fr = 3.14159265358979f * exp2f(0.4f * float(r));
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            float s, c;
+            __sincosf(fr * u[i], &s, &c);
+#pragma unroll
+            for (int k = r; k < kFreq; k += 5) {
+                put(3 + (k * 3 + i) * 2, s);
+                put(3 + (k * 3 + i) * 2 + 1, c);
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {   // angle x 4
+                    float s2 = 2.0f * s * c, c2 = 1.0f - 2.0f * s * s;
+                    s = s2;
+                    c = c2;
+                }
+            }
+        }
+    }
+}
+
+// Forward pass of the CTA's 128 rows: every thread passes its row's
+// normalised point and gets the row's output (label units).  `phase` is the
+// parity of the next mbarrier phase (the same in every thread).  If an MMA
+// does not complete within kMmaWaitNs, every thread gets fail = true and 0.
+__device__ __forceinline__ float tc_forward(TcSmem &sm, uint32_t &phase, const float u[3], bool &fail) {
+    const int t = threadIdx.x;
+    const uint32_t act = umma::smem_u32(sm.act);
+    {
+        uint32_t f[kInPad / 2];
+        feature_pairs(u, f);
+#pragma unroll
+        for (int kc = 0; kc < kInPad / 8; ++kc) umma::st_shared_v4(act + act_offset(t, kc), f[4 * kc], f[4 * kc + 1], f[4 * kc + 2], f[4 * kc + 3]);
+    }
+    const uint32_t row_taddr = sm.tmem + (uint32_t(t & ~31) << 16);   // this warp's 32 lanes
+    float out = 0.0f;
+#pragma unroll 1
+    for (int L = 0; L < kHidden; ++L) {
+        umma::fence_smem_to_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (t == 0) {
+            umma::fence_after_sync();
+            const int ksteps = (L == 0 ? kInPad : kHid) / 16;
+            const uint32_t b = umma::smem_u32(L == 0 ? sm.w0 : sm.w[L - 1]);
+            for (int j = 0; j < ksteps; ++j)
+                umma::mma_bf16(sm.tmem, umma::smem_desc(act + uint32_t(j) * 2u * kActK, kActK, kCore),
+                               umma::smem_desc(b + uint32_t(j) * 2u * kWK, kWK, kCore), kTcIdesc, uint32_t(j));
+            umma::mma_commit(&sm.bar);
+        }
+        const int late = t == 0 ? int(!umma::mbar_wait(&sm.bar, phase, kMmaWaitNs)) : 0;
+        phase ^= 1u;
+        if (__syncthreads_or(late)) {
+            fail = true;
+            return 0.0f;
+        }
+        umma::fence_after_sync();
+        __syncwarp();
+        uint32_t r[64];
+        umma::tmem_ld64(row_taddr, r);
+        const float *bias = sm.b[L];
+        if (L + 1 < kHidden) {
+#pragma unroll
+            for (int kc = 0; kc < kHid / 8; ++kc) {
+                uint32_t h[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = kc * 8 + q * 2;
+                    h[q] = silu2_bf16(__uint_as_float(r[c]) + bias[c], __uint_as_float(r[c + 1]) + bias[c + 1]);
+                }
+                umma::st_shared_v4(act + act_offset(t, kc), h[0], h[1], h[2], h[3]);
+            }
+        } else {
+            // Output layer: dot product of the (bf16-rounded) last activations with W4.
+#pragma unroll
+            for (int c = 0; c < kHid; c += 2) {
+                const uint32_t h = silu2_bf16(__uint_as_float(r[c]) + bias[c], __uint_as_float(r[c + 1]) + bias[c + 1]);
+                out += __uint_as_float(h << 16) * sm.w4[c] + __uint_as_float(h & 0xffff0000u) * sm.w4[c + 1];
+            }
+            out += sm.b4;
+        }
+    }
+    return out;
+}
+
+}  // namespace mlp
+}  // namespace fpt

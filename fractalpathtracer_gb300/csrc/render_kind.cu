@@ -55,15 +55,24 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         march_blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
     int skip_blocks = 0;
+    const bool skip_tc = skip_pass && pl.skip->engine == kNetTcgen05;
     if (skip_pass) {
         static bool attr = false;
         if (!attr) {
             cudaFuncSetAttribute(skip_march_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(skip_smem_bytes()));
+            cudaFuncSetAttribute(skip_march_tc_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mlp::tc_smem_bytes()));
             attr = true;
         }
         int skip_per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&skip_per_sm, skip_march_kernel<KIND>, 32 * kSkipWarps, skip_smem_bytes());
+        if (skip_tc)
+            skip_per_sm = mlp::tc_blocks_per_sm(reinterpret_cast<const void *>(skip_march_tc_kernel<KIND>));
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&skip_per_sm, skip_march_kernel<KIND>, 32 * kSkipWarps, skip_smem_bytes());
         skip_blocks = sms * (skip_per_sm > 0 ? skip_per_sm : 1);
+    }
+    if (pl.grids) {
+        pl.grids[0] = uint32_t(march_blocks);
+        pl.grids[1] = uint32_t(skip_blocks);
     }
     int shade_per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_per_sm, shade_kernel<KIND>, 128, 0);
@@ -92,7 +101,10 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
             // the camera rays only, the box clip applies in every pass.
             if (skip_pass && b == 0u)
                 timed(KC_SKIP, [&] {
-                    skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, cur, *pl.skip);
+                    if (skip_tc)
+                        skip_march_tc_kernel<KIND><<<skip_blocks, mlp::kTcRows, mlp::tc_smem_bytes(), stream>>>(W, cur, *pl.skip);
+                    else
+                        skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, cur, *pl.skip);
                 });
             timed(KC_MARCH, [&] {
                 if (interleaved) march_ilv_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
@@ -149,7 +161,13 @@ cudaError_t FPT_CAT(launch_skip_primary_k, FPT_KIND)(const DeviceScene *scene, u
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(skip_primary_kernel<FPT_KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(skip_smem_bytes()));
+        cudaFuncSetAttribute(skip_primary_tc_kernel<FPT_KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mlp::tc_smem_bytes()));
         attr = true;
+    }
+    if (args.engine == kNetTcgen05) {
+        const uint32_t blocks = (W * H + uint32_t(mlp::kTcRows) - 1u) / uint32_t(mlp::kTcRows);
+        skip_primary_tc_kernel<FPT_KIND><<<blocks, mlp::kTcRows, mlp::tc_smem_bytes(), st>>>(scene, args, hits);
+        return cudaGetLastError();
     }
     const uint32_t warps = (W * H + 31u) / 32u;
     const uint32_t blocks = (warps + kSkipWarps - 1u) / kSkipWarps;

@@ -16,13 +16,15 @@
 // Geometry lies inside the model's box: a ray that misses or leaves it is a
 // miss without further evaluation.
 //
-// The network runs on the tensor cores one warp at a time (32 rows), so the
-// loop is warp-synchronous: every iteration each lane adds one network row
-// and one exact evaluation.
+// Two network engines: tcgen05 (default; 128 rows per CTA, accumulators in
+// tensor memory, a CTA-synchronous loop) and mma.sync (32 rows per warp, a
+// warp-synchronous loop).  Every iteration each lane adds one network row and
+// one exact evaluation.
 #pragma once
 
 #include "fpt_march.cuh"
 #include "mlp.cuh"
+#include "mlp_tc.cuh"
 #include "wavefront.cuh"
 
 namespace fpt {
@@ -34,12 +36,15 @@ struct SkipArgs {
     float safety;                // scale of the predicted distance in a proposal
     uint32_t max_iters;          // skip iterations per ray before hand-over
     uint32_t use_network;        // 0: box clip only (the march kernel applies it; no skip pass)
+    uint32_t engine;             // network engine: kNetTcgen05 or kNetMmaSync
+    uint32_t *guard;             // primary-ray pass: error word (bit 2: an MMA did not complete), or null
     unsigned long long *stats;   // kSkipStats counters or null
 };
 
 enum SkipStat : int { SK_ROWS = 0, SK_FORWARDS = 1, SK_EXACT = 2, SK_ACCEPT = 3, SK_REJECT = 4, SK_ESCAPE = 5, SK_HANDOVER = 6,
                       SK_DIST = 7, kSkipStats = 8 };
 
+constexpr uint32_t kNetTcgen05 = 0, kNetMmaSync = 1;
 constexpr int kSkipWarps = 4;
 inline size_t skip_smem_bytes() { return ((sizeof(mlp::SmemWeights) + 127) & ~size_t(127)) + kSkipWarps * sizeof(mlp::WarpForward); }
 
@@ -93,26 +98,27 @@ __device__ __forceinline__ bool skip_begin(SkipLane &L, const SkipArgs &A, float
 
 enum SkipOutcome : int { SO_CONTINUE = 0, SO_HANDOVER = 1, SO_ESCAPE = 2 };
 
-// One warp-synchronous iteration for all 32 lanes (every lane must call it;
-// lanes with phase SP_IDLE only lend their network row).
-template <int KIND>
-__device__ __forceinline__ int skip_step(SkipLane &L, const DeviceScene &S, const SkipArgs &A, const mlp::SmemWeights &sw,
-                                         mlp::WarpForward &wf, int lane, uint32_t &c_rows, uint32_t &c_fwd, uint32_t &c_exact,
-                                         uint32_t &c_acc, uint32_t &c_rej) {
-    const unsigned FULL = 0xffffffffu;
+// The network query of a lane in SP_PROPOSE: the look-ahead point p + lam d
+// dir, normalised to the model box (other lanes query their position; the
+// row is computed but not used).  Returns whether the lane proposes.
+__device__ __forceinline__ bool skip_query(const SkipLane &L, const SkipArgs &A, float u[3]) {
     const bool propose = A.use_network && L.phase == SP_PROPOSE;
-    float3 p = L.origin + L.dir * L.t;
-    float m = 0.0f;
-    if (__any_sync(FULL, propose)) {
-        float3 q0 = propose ? p + L.dir * (L.lam * L.d) : p;
-        float u[3] = {(q0.x - A.M.center[0]) * A.M.inv_half[0], (q0.y - A.M.center[1]) * A.M.inv_half[1],
-                      (q0.z - A.M.center[2]) * A.M.inv_half[2]};
+    const float3 p = L.origin + L.dir * L.t;
+    const float3 q0 = propose ? p + L.dir * (L.lam * L.d) : p;
+    u[0] = (q0.x - A.M.center[0]) * A.M.inv_half[0];
+    u[1] = (q0.y - A.M.center[1]) * A.M.inv_half[1];
+    u[2] = (q0.z - A.M.center[2]) * A.M.inv_half[2];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) u[k] = fminf(fmaxf(u[k], -4.0f), 4.0f);
-        m = mlp::forward32(sw, wf, u, lane) * A.M.label_scale;
-        if (lane == 0) ++c_fwd;
-        if (propose) ++c_rows;
-    }
+    for (int k = 0; k < 3; ++k) u[k] = fminf(fmaxf(u[k], -4.0f), 4.0f);
+    return propose;
+}
+
+// The rest of an iteration once the network distance m (world units) of a
+// proposing lane is known: the proposal, its certification by one exact
+// evaluation, and the hand-over / escape decision.
+template <int KIND>
+__device__ __forceinline__ int skip_advance(SkipLane &L, const DeviceScene &S, const SkipArgs &A, bool propose, float m,
+                                            uint32_t &c_exact, uint32_t &c_acc, uint32_t &c_rej) {
     if (L.phase == SP_IDLE) return SO_CONTINUE;
     bool cand = false;
     float s = 0.0f;
@@ -155,6 +161,23 @@ __device__ __forceinline__ int skip_step(SkipLane &L, const DeviceScene &S, cons
     return SO_CONTINUE;
 }
 
+// One warp-synchronous iteration for all 32 lanes (every lane must call it;
+// lanes with phase SP_IDLE only lend their network row).
+template <int KIND>
+__device__ __forceinline__ int skip_step(SkipLane &L, const DeviceScene &S, const SkipArgs &A, const mlp::SmemWeights &sw,
+                                         mlp::WarpForward &wf, int lane, uint32_t &c_rows, uint32_t &c_fwd, uint32_t &c_exact,
+                                         uint32_t &c_acc, uint32_t &c_rej) {
+    float u[3];
+    const bool propose = skip_query(L, A, u);
+    float m = 0.0f;
+    if (__any_sync(0xffffffffu, propose)) {
+        m = mlp::forward32(sw, wf, u, lane) * A.M.label_scale;
+        if (lane == 0) ++c_fwd;
+        if (propose) ++c_rows;
+    }
+    return skip_advance<KIND>(L, S, A, propose, m, c_exact, c_acc, c_rej);
+}
+
 __device__ __forceinline__ void skip_flush_stats(const SkipArgs &A, int lane, uint32_t rows, uint32_t fwd, uint32_t exact,
                                                  uint32_t acc, uint32_t rej, uint32_t esc, uint32_t hand) {
     if (!A.stats) return;
@@ -167,12 +190,81 @@ __device__ __forceinline__ void skip_flush_stats(const SkipArgs &A, int lane, ui
     }
 }
 
+// Takes jobs for the warp's idle lanes (warp-synchronous: one atomic per warp
+// per try).  Rays that miss the box are resolved at once and the lane draws
+// again.
+__device__ __forceinline__ void skip_refill(SkipLane &L, const SkipArgs &A, const WaveParams &W, int cur, uint32_t n_path,
+                                            uint32_t total, int lane, bool &retired, uint32_t &job, bool &shadow, uint32_t &c_esc) {
+    const unsigned FULL = 0xffffffffu;
+    for (int tries = 0; tries < 4; ++tries) {
+        const bool need = L.phase == SP_IDLE && !retired;
+        unsigned ballot = __ballot_sync(FULL, need);
+        if (!ballot) break;
+        uint32_t leader = __ffs(ballot) - 1, base = 0;
+        if (lane == int(leader)) base = atomicAdd(&W.counters[C_SKIP], (unsigned)__popc(ballot));
+        base = __shfl_sync(FULL, base, leader);
+        if (need) {
+            uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
+            if (idx >= total) {
+                retired = true;
+            } else {
+                shadow = idx >= n_path;
+                float3 o, d;
+                if (!shadow) {
+                    job = W.q_march[cur][idx];
+                    const PathRec &R = W.paths[job];
+                    o = mk3(R.pos.x, R.pos.y, R.pos.z);
+                    d = mk3(R.dir.x, R.dir.y, R.dir.z);
+                } else {
+                    job = idx - n_path;
+                    const ShadowJob &J = W.q_shadow[cur][job];
+                    o = mk3(J.origin.x, J.origin.y, J.origin.z) + mk3(J.normal.x, J.normal.y, J.normal.z) * 0.001f;
+                    d = mk3(J.dir.x, J.dir.y, J.dir.z);
+                }
+                if (!skip_begin(L, A, o, d)) {
+                    ++c_esc;
+                    if (!shadow) W.paths[job].color.w = bitsf(fbits(W.paths[job].color.w) | PF_ESCAPED);
+                    else W.q_shadow[cur][job].dir.w = 1.0f;
+                }
+            }
+        }
+    }
+}
+
+// Writes the outcome of a lane whose skip ended (escape or hand-over) and
+// idles the lane.
+__device__ __forceinline__ void skip_finish(SkipLane &L, const WaveParams &W, int cur, int out, uint32_t job, bool shadow,
+                                            uint32_t &c_esc, uint32_t &c_hand) {
+    if (out == SO_ESCAPE) ++c_esc; else ++c_hand;
+    const bool known = out == SO_HANDOVER && L.phase == SP_PROPOSE;   // L.d is the exact distance here
+    if (!shadow) {
+        PathRec &R = W.paths[job];
+        float3 p = L.origin + L.dir * L.t;
+        R.pos = make_float4(p.x, p.y, p.z, R.pos.w);
+        if (out == SO_ESCAPE) R.color.w = bitsf(fbits(R.color.w) | PF_ESCAPED);
+        if (known) {
+            R.grad.w = L.d;
+            R.color.w = bitsf(fbits(R.color.w) | PF_KNOWN_D);
+        }
+    } else {
+        ShadowJob &J = W.q_shadow[cur][job];
+        J.normal.w = L.t;
+        if (out == SO_ESCAPE) J.dir.w = 1.0f;
+        if (known) {
+            J.contrib.w = L.d;
+            J.dir.w = 2.0f;
+        }
+    }
+    L.phase = SP_IDLE;
+}
+
 // Wavefront pass: advances the path rays of q_march[cur] and the shadow
 // rays of q_shadow[cur] before the exact march kernel takes them.  Path rays
 // move R.pos; escapes set PF_ESCAPED (the march kernel then classifies them
 // as misses without evaluating).  Shadow rays keep their advance in
 // normal.w; escapes set dir.w = 1 (unoccluded).  Jobs are taken with
-// per-lane regeneration from counter C_SKIP.
+// per-lane regeneration from counter C_SKIP.  Network on mma.sync, one warp
+// (32 rows) at a time.
 template <int KIND>
 __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WaveParams W, int cur, SkipArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -198,70 +290,64 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WavePara
     const unsigned long long t0 = global_ns();
     while (true) {
         if (loop_guard(trips, t0, W.counters)) break;
-        // Refill idle lanes (one atomic per warp); rays that miss the box are
-        // resolved at once and the lane draws again.
-        for (int tries = 0; tries < 4; ++tries) {
-            const bool need = L.phase == SP_IDLE && !retired;
-            unsigned ballot = __ballot_sync(FULL, need);
-            if (!ballot) break;
-            uint32_t leader = __ffs(ballot) - 1, base = 0;
-            if (lane == uint32_t(leader)) base = atomicAdd(&W.counters[C_SKIP], (unsigned)__popc(ballot));
-            base = __shfl_sync(FULL, base, leader);
-            if (need) {
-                uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
-                if (idx >= total) {
-                    retired = true;
-                } else {
-                    shadow = idx >= n_path;
-                    float3 o, d;
-                    if (!shadow) {
-                        job = W.q_march[cur][idx];
-                        const PathRec &R = W.paths[job];
-                        o = mk3(R.pos.x, R.pos.y, R.pos.z);
-                        d = mk3(R.dir.x, R.dir.y, R.dir.z);
-                    } else {
-                        job = idx - n_path;
-                        const ShadowJob &J = W.q_shadow[cur][job];
-                        o = mk3(J.origin.x, J.origin.y, J.origin.z) + mk3(J.normal.x, J.normal.y, J.normal.z) * 0.001f;
-                        d = mk3(J.dir.x, J.dir.y, J.dir.z);
-                    }
-                    if (!skip_begin(L, A, o, d)) {
-                        ++c_esc;
-                        if (!shadow) W.paths[job].color.w = bitsf(fbits(W.paths[job].color.w) | PF_ESCAPED);
-                        else W.q_shadow[cur][job].dir.w = 1.0f;
-                    }
-                }
-            }
-        }
+        skip_refill(L, A, W, cur, n_path, total, lane, retired, job, shadow, c_esc);
         if (!__any_sync(FULL, L.phase != SP_IDLE)) {
             if (__all_sync(FULL, retired)) break;
             continue;
         }
         const int out = skip_step<KIND>(L, S, A, sw, wf, lane, c_rows, c_fwd, c_exact, c_acc, c_rej);
-        if (L.phase != SP_IDLE && out != SO_CONTINUE) {
-            if (out == SO_ESCAPE) ++c_esc; else ++c_hand;
-            const bool known = out == SO_HANDOVER && L.phase == SP_PROPOSE;   // L.d is the exact distance here
-            if (!shadow) {
-                PathRec &R = W.paths[job];
-                float3 p = L.origin + L.dir * L.t;
-                R.pos = make_float4(p.x, p.y, p.z, R.pos.w);
-                if (out == SO_ESCAPE) R.color.w = bitsf(fbits(R.color.w) | PF_ESCAPED);
-                if (known) {
-                    R.grad.w = L.d;
-                    R.color.w = bitsf(fbits(R.color.w) | PF_KNOWN_D);
-                }
-            } else {
-                ShadowJob &J = W.q_shadow[cur][job];
-                J.normal.w = L.t;
-                if (out == SO_ESCAPE) J.dir.w = 1.0f;
-                if (known) {
-                    J.contrib.w = L.d;
-                    J.dir.w = 2.0f;
-                }
-            }
-            L.phase = SP_IDLE;
-        }
+        if (L.phase != SP_IDLE && out != SO_CONTINUE) skip_finish(L, W, cur, out, job, shadow, c_esc, c_hand);
     }
+    skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
+}
+
+// The same pass with the network on the 5th-generation tensor cores: the
+// loop is CTA-synchronous, and each iteration in which any lane of the
+// 128-thread CTA proposes runs one 128-row forward pass (mlp::tc_forward).
+// Guard word bits: 1 = loop time limit, 2 = an MMA did not complete.
+template <int KIND>
+__global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WaveParams W, int cur, SkipArgs A) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
+    const DeviceScene &S = *W.scene;
+    const uint32_t n_path = W.counters[C_MARCH0 + cur];
+    const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
+    if (total == 0u) return;
+    mlp::tc_setup(sm, A.M);
+    const int lane = threadIdx.x & 31;
+    SkipLane L;
+    L.phase = SP_IDLE;
+    bool retired = false, shadow = false, fail = false;
+    uint32_t job = 0, phase = 0;
+    uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
+    uint32_t trips = 0;
+    const unsigned long long t0 = global_ns();
+    while (true) {
+        if ((++trips & 1023u) == 0u) {   // the same trip in every thread
+            if (__syncthreads_or(global_ns() - t0 > kLoopLimitNs)) {
+                if (threadIdx.x == 0) atomicOr(W.counters + C_GUARD, 1u);
+                break;
+            }
+        }
+        skip_refill(L, A, W, cur, n_path, total, lane, retired, job, shadow, c_esc);
+        if (!__syncthreads_or(L.phase != SP_IDLE)) {
+            if (__syncthreads_and(retired)) break;
+            continue;
+        }
+        float u[3];
+        const bool propose = skip_query(L, A, u);
+        float m = 0.0f;
+        if (__syncthreads_or(propose)) {
+            m = mlp::tc_forward(sm, phase, u, fail) * A.M.label_scale;
+            if (fail) break;   // the same in every thread
+            if (lane == 0) ++c_fwd;
+            if (propose) ++c_rows;
+        }
+        const int out = skip_advance<KIND>(L, S, A, propose, m, c_exact, c_acc, c_rej);
+        if (L.phase != SP_IDLE && out != SO_CONTINUE) skip_finish(L, W, cur, out, job, shadow, c_esc, c_hand);
+    }
+    mlp::tc_teardown(sm);
+    if (fail && threadIdx.x == 0) atomicOr(W.counters + C_GUARD, 2u);
     skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
 }
 
@@ -326,6 +412,79 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_primary_kernel(const 
         }
         hits[i] = h;
     }
+    skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
+}
+
+// skip_primary_kernel with the network on tcgen05: 128 pixels per CTA
+// iteration, CTA-synchronous skip loop.
+template <int KIND>
+__global__ void __launch_bounds__(mlp::kTcRows, 3) skip_primary_tc_kernel(const DeviceScene *scene, SkipArgs A,
+                                                                          FptCudaPrimaryHit *hits) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
+    const DeviceScene &S = *scene;
+    mlp::tc_setup(sm, A.M);
+    const int lane = threadIdx.x & 31;
+    const uint32_t pixels = S.width * S.height;
+    uint32_t phase = 0;
+    bool fail = false;
+    uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
+    for (uint32_t base = blockIdx.x * uint32_t(mlp::kTcRows); base < pixels; base += gridDim.x * uint32_t(mlp::kTcRows)) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < pixels;
+        const uint32_t gx = valid ? i % S.width : 0u, gy = valid ? i / S.width : 0u;
+        float2 uv = screen_uv(gx, gy, S);
+        PathRng rng;
+        rng.init(false, 0u, 0u, 0u, uv.x, uv.y);
+        float3 rp = mk3(0.f), dr = mk3(0.f, 0.f, 1.f);
+        bool ray = valid && camera_ray(S, uv, rng, false, rp, dr);
+        SkipLane L;
+        L.phase = SP_IDLE;
+        bool escaped = false;
+        uint32_t exact0 = c_exact;
+        if (ray && !skip_begin(L, A, rp, dr)) escaped = true;
+        while (__syncthreads_or(L.phase != SP_IDLE)) {
+            float u[3];
+            const bool propose = skip_query(L, A, u);
+            float m = 0.0f;
+            if (__syncthreads_or(propose)) {
+                m = mlp::tc_forward(sm, phase, u, fail) * A.M.label_scale;
+                if (fail) break;   // the same in every thread
+                if (lane == 0) ++c_fwd;
+                if (propose) ++c_rows;
+            }
+            const int out = skip_advance<KIND>(L, S, A, propose, m, c_exact, c_acc, c_rej);
+            if (L.phase != SP_IDLE && out != SO_CONTINUE) {
+                if (out == SO_ESCAPE) { escaped = true; ++c_esc; } else ++c_hand;
+                L.phase = SP_IDLE;
+            }
+        }
+        if (fail) break;
+        if (!valid) continue;
+        FptCudaPrimaryHit h;
+        h.distance = 0.0f; h.normal[0] = h.normal[1] = h.normal[2] = 0.0f; h.steps = 0; h.hit = 0;
+        if (ray) {
+            if (escaped) {
+                h.distance = S.render[4];
+                h.steps = c_exact - exact0;
+            } else {
+                float3 start = L.origin + L.dir * L.t;
+                March m = march_loop<KIND>(S, start, dr, int(S.render[1]), S.render[3], 0.0002f);
+                float travel = len3(m.pos - rp);
+                bool hit = m.found && isfinite(travel) && travel < S.render[4] * 0.99f;
+                h.distance = travel;
+                h.steps = uint32_t(m.steps) + (c_exact - exact0);
+                h.hit = hit ? 1u : 0u;
+                if (hit) {
+                    float3 n = normal_direct<KIND>(m.pos, S);
+                    h.normal[0] = n.x; h.normal[1] = n.y; h.normal[2] = n.z;
+                }
+            }
+        }
+        hits[i] = h;
+    }
+    mlp::tc_teardown(sm);
+    if (fail && threadIdx.x == 0 && A.guard) atomicOr(A.guard, 2u);
     skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
 }
 

@@ -26,6 +26,7 @@ EXPORTED = [
     "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
     "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch", "fpt_cuda_set_launch_shape",
     "fpt_cuda_set_march_schedule",
+    "fpt_cuda_set_network_engine",
 ]
 
 

@@ -38,7 +38,8 @@ class FptCudaSkipStats(C.Structure):
 class FptCudaRenderStats(C.Structure):
     _fields_ = [("kernel_launches", C.c_uint64), ("march_launches", C.c_uint64), ("shade_launches", C.c_uint64),
                 ("skip_launches", C.c_uint64), ("march_evals", C.c_uint64), ("shade_evals", C.c_uint64),
-                ("march_ms", C.c_double), ("shade_ms", C.c_double), ("skip_ms", C.c_double), ("total_ms", C.c_double)]
+                ("march_ms", C.c_double), ("shade_ms", C.c_double), ("skip_ms", C.c_double), ("total_ms", C.c_double),
+                ("march_grid", C.c_uint32), ("skip_grid", C.c_uint32)]
 
 
 class FptCudaBatchStats(C.Structure):
@@ -87,6 +88,7 @@ def declare(L: C.CDLL) -> None:
     L.fpt_cuda_render_stats.argtypes = [P(FptCudaRenderStats)]
     L.fpt_cuda_set_launch_shape.argtypes = [C.c_uint32, C.c_int32]
     L.fpt_cuda_set_march_schedule.argtypes = [C.c_uint32, C.c_uint32]
+    L.fpt_cuda_set_network_engine.argtypes = [C.c_uint32]
     L.fpt_cuda_render_batch.argtypes = [cfg, ext, C.c_size_t, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_size_t,
                                         P(FptCudaBatchStats)] + err
     L.fpt_cuda_autotune_batch.argtypes = [cfg, ext, C.c_size_t, C.c_uint32, P(FptCudaTuneResult)] + err
@@ -94,7 +96,7 @@ def declare(L: C.CDLL) -> None:
                  "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
                  "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
                  "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch", "fpt_cuda_set_launch_shape",
-                 "fpt_cuda_set_march_schedule"):
+                 "fpt_cuda_set_march_schedule", "fpt_cuda_set_network_engine"):
         getattr(L, name).restype = C.c_int
 
 
@@ -306,6 +308,17 @@ def autotune_batch(bundles, rounds=3) -> dict:
 def set_launch_shape(wave_paths: int = 0, march_blocks: int = 0) -> None:
     from .native import lib
     lib().fpt_cuda_set_launch_shape(wave_paths, march_blocks)
+
+
+NET_TCGEN05 = 0
+NET_MMA_SYNC = 1
+
+
+def set_network_engine(engine: int = NET_TCGEN05) -> None:
+    """Surrogate network engine of later skip passes and predictions: NET_TCGEN05 (default) or NET_MMA_SYNC."""
+    from .native import lib
+    if lib().fpt_cuda_set_network_engine(engine) != 0:
+        raise ValueError("engine must be NET_TCGEN05 (0) or NET_MMA_SYNC (1)")
 
 
 def set_march_schedule(schedule: int = 0, batch: int = 0) -> None:

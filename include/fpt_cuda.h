@@ -837,6 +837,8 @@ struct FptCudaRenderStats {
     double shade_ms;
     double skip_ms;
     double total_ms;             /* the call's elapsed_ms */
+    uint32_t march_grid;         /* blocks of the persistent march kernel */
+    uint32_t skip_grid;          /* blocks of the persistent skip kernel (0: no skip pass) */
 };
 int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
 
@@ -855,6 +857,15 @@ int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks);
  * rounding; on the power-8 Mandelbulb at 1080p the interleaved march took
  * 48-60 ms against 36 ms for lockstep. */
 int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch);
+
+/* Engine of the surrogate network in later skip passes and predictions:
+ * FPT_CUDA_NET_TCGEN05 (default: 5th-generation tensor cores, 128 rows per
+ * CTA, accumulators in tensor memory) or FPT_CUDA_NET_MMA_SYNC (warp-level
+ * mma.sync, 32 rows per warp).  Both compute the same network; outputs differ
+ * only in the order of the FP32 sums.  Returns 1 for an unknown engine. */
+#define FPT_CUDA_NET_TCGEN05 0u
+#define FPT_CUDA_NET_MMA_SYNC 1u
+int fpt_cuda_set_network_engine(uint32_t engine);
 
 /* ---- Batched scenes (no counterpart in the reference; its render-batch
  * command only reuses the process, src/main.rs:2269) ----

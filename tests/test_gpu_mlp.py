@@ -1,6 +1,7 @@
 """Learned distance surrogate on the GPU.
 
-* Forward pass and gradients of the BF16 tensor-core kernels against the FP64
+* Forward pass (tcgen05 and mma.sync engines) and gradients of the BF16
+  tensor-core kernels against the FP64
   oracle that rounds to BF16 where the kernels store BF16 (the remaining
   differences: FP32 accumulation order, the hardware tanh/sin/cos, BF16
   rounding-boundary flips; inference takes its sigmoid from an f16x2 tanh).
@@ -45,19 +46,49 @@ def blank_model(native):
     nx.mlp_destroy(h)
 
 
-def test_forward_matches_oracle(blank_model):
+@pytest.fixture
+def engine(request):
+    nx.set_network_engine(request.param)
+    yield request.param
+    nx.set_network_engine(nx.NET_TCGEN05)
+
+
+ENGINES = [pytest.param(nx.NET_TCGEN05, id="tcgen05"), pytest.param(nx.NET_MMA_SYNC, id="mma_sync")]
+
+
+@pytest.mark.parametrize("engine", ENGINES, indirect=True)
+def test_forward_matches_oracle(blank_model, engine):
     params = scenes.random_mlp_params(11)
     nx.mlp_set_params(blank_model, params)
     back = nx.mlp_get_params(blank_model)
     assert np.array_equal(back, params)
-    pts = _points(4096, 5)
+    pts = _points(4096 + 77, 5)   # a ragged last tile
     y = nx.mlp_predict(blank_model, pts).astype(np.float64)
     ref = oracle.mlp_forward(params, *BULB_BOX, pts, emulate_bf16=True)
     err = np.abs(y - ref)
     scale = np.abs(ref).max() + 0.1
-    print(f"forward: max|y| {np.abs(ref).max():.3f} p99 err {np.percentile(err, 99):.2e} max err {err.max():.2e}")
+    print(f"forward ({engine}): max|y| {np.abs(ref).max():.3f} p99 err {np.percentile(err, 99):.2e} max err {err.max():.2e}")
     assert np.percentile(err, 99) <= 3e-3 * scale
     assert err.max() <= 1.5e-2 * scale
+
+
+def test_engines_agree(blank_model):
+    """tcgen05 and mma.sync compute the same network; only FP32 summation order differs (and BF16 rounding flips
+    of activations that it moves across a rounding boundary)."""
+    params = scenes.random_mlp_params(12)
+    nx.mlp_set_params(blank_model, params)
+    pts = _points(1 << 16, 6)
+    try:
+        nx.set_network_engine(nx.NET_MMA_SYNC)
+        y_mma = nx.mlp_predict(blank_model, pts).astype(np.float64)
+    finally:
+        nx.set_network_engine(nx.NET_TCGEN05)
+    y_tc = nx.mlp_predict(blank_model, pts).astype(np.float64)
+    d = np.abs(y_tc - y_mma)
+    scale = np.abs(y_mma).max() + 0.1
+    print(f"tcgen05 vs mma.sync: identical {np.mean(d == 0):.4f} p99 {np.percentile(d, 99):.2e} max {d.max():.2e}")
+    assert np.percentile(d, 99) <= 1e-3 * scale
+    assert d.max() <= 1e-2 * scale
 
 
 def test_gradients_match_oracle(blank_model):
@@ -111,7 +142,8 @@ def _hits(native, cfg, ext):
     return hits, ms
 
 
-def test_skip_march_keeps_hits(trained_bulb, native):
+@pytest.mark.parametrize("engine", ENGINES, indirect=True)
+def test_skip_march_keeps_hits(trained_bulb, native, engine):
     h, _ = trained_bulb
     cfg, ext = scenes.mandelbulb_primary(320, 240)
     plain, _ = _hits(native, cfg, ext)
