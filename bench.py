@@ -151,11 +151,11 @@ SFU_PEAK_TOPS = 152 * 16 * 2.070e9 / 1e12
 MLP_FLOP = 2 * (99 * 64 + 3 * 64 * 64 + 64)              # one network row (37.3 kFLOP)
 
 
-def surrogate_config():
+def surrogate_config(scene: str = "mandelbulb"):
     """Training recipe of the learned skip: 16M points labelled by the exact DE (50% uniform in the
     box, 50% within 0.05 of the surface), asymmetric loss with 10x weight on overestimates."""
     from fractalpathtracer_gb300 import native_ext as nx, scenes
-    lo, hi = scenes.SURROGATE_BOXES["mandelbulb"]
+    lo, hi = scenes.SURROGATE_BOXES[scene]
     return nx.mlp_config(lo, hi, points=1 << 24, near_fraction=0.5, near_band=0.05, batch=16384, steps=4000,
                          lr=2e-3, overestimate_weight=10.0, seed=1)
 
@@ -400,6 +400,31 @@ def other_configs(native, nx, scenes, peaks):
         "render_ms": ms, "Mrays_per_s": 2 * hits.size / ms / 1e3, "cells_visited": cells,
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                      "work": "7 B per visited cell + 32 B per pixel"}}
+    # The learned skip on the Mandelbox (scale -1.5, 12 iterations): the same recipe, its own model.
+    b = scenes.mandelbox_path(W, H, SPP, BOUNCES)
+    model, train = nx.mlp_create(b.cfg, b.ext, surrogate_config("mandelbox"))
+    arms = {}
+    for name, mode in (("plain", 0), ("skip", 1), ("box_only", 2)):
+        e = ffi_copy(b.ext)
+        if mode:
+            e.surrogate, e.surrogate_model = mode, model
+        for _ in range(2):
+            native.cuda_render(b.cfg, e, linear=False)
+        ms = med([native.cuda_render(b.cfg, e, linear=False)[2] for _ in range(3)])
+        arms[name] = {"ms": ms, "Mpaths_per_s": W * H * SPP / ms / 1e3}
+        if mode == 1:
+            arms[name]["skip_stats"] = nx.skip_stats()
+            hp, _ = native.trace_primary(b.cfg, b.ext)
+            hs, _ = native.trace_primary(b.cfg, e)
+            both = (hp["hit"] > 0) & (hs["hit"] > 0)
+            dt = np.abs(hp["distance"][both].astype(np.float64) - hs["distance"][both]) / (1.0 + hp["distance"][both])
+            arms[name]["hit_agreement"] = float(((hp["hit"] > 0) == (hs["hit"] > 0)).mean())
+            arms[name]["p99_rel_dist_delta"] = float(np.percentile(dt, 99)) if dt.size else None
+    nx.mlp_destroy(model)
+    arms["skip_over_plain"] = arms["skip"]["Mpaths_per_s"] / arms["plain"]["Mpaths_per_s"]
+    arms["train_ms"] = train["train_ms"]
+    arms["loss_last"] = train["loss_last"]
+    out[f"mandelbox_skip_{W}x{H}_{SPP}spp"] = arms
     return out
 
 

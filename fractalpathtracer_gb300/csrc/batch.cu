@@ -140,7 +140,7 @@ bool upload_plan(const BatchPlan &P, uint32_t wave_paths, char *error, size_t er
         !ensure_buffer((void **)&B.tables, &B.cap_tables, (2 * (n + 1) + 1) * sizeof(uint32_t), error, error_len) ||
         !ensure_buffer((void **)&B.accum, &B.cap_accum, P.pixels * sizeof(float4), error, error_len) ||
         !ensure_buffer((void **)&B.sample_rgb, &B.cap_sample, P.pixels * sizeof(float4), error, error_len) ||
-        !ensure_buffer(&c.wave, &c.cap_wave, size_t(wave_paths) * kWaveBytesPerPath, error, error_len) ||
+        !ensure_buffer(&c.wave, &c.cap_wave, wave_scratch_bytes(wave_paths), error, error_len) ||
         !ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len))
         return false;
     std::vector<uint32_t> tables(2 * (n + 1) + 1, 0u);
@@ -184,6 +184,8 @@ uint32_t launch_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_pa
     W.q_march[0] = reinterpret_cast<uint32_t *>(base + size_t(cap) * (96 + 128));
     W.q_march[1] = W.q_march[0] + cap;
     W.q_shade = W.q_march[1] + cap;
+    W.q_skip = nullptr;
+    W.skip_queue = 0u;
     int sms = 0, dev = 0, per_sm = 0, shade_per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -211,6 +211,7 @@ bool compile_scene(const FptRenderConfig &c, const FptCudaSceneExt *ext_in, Devi
     S.surrogate = e.surrogate;
     S.surrogate_margin = e.surrogate_margin;
     S.surrogate_safety = e.surrogate_safety;
+    S.surrogate_max_iters = e.surrogate_max_iters;
     if (e.formula == FPT_CUDA_FORMULA_MANDELBOX && !(S.box_min2 > 0.0f)) {
         set_error(error, error_len, "Mandelbox minimum radius must be positive");
         return false;
@@ -370,7 +371,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         size_t cap = c.wave_paths ? c.wave_paths : (size_t(64) << 20);   // one wave per 1080p 16 spp frame
         cap = std::min(cap, per_launch);
         pl.wave_paths = uint32_t(cap);
-        if (!ensure_buffer(&c.wave, &c.cap_wave, cap * kWaveBytesPerPath, error, error_len)) return 1;
+        if (!ensure_buffer(&c.wave, &c.cap_wave, wave_scratch_bytes(cap), error, error_len)) return 1;
         pl.wave_scratch = c.wave;
     }
     pl.sample_rgb = c.sample_rgb;
@@ -549,6 +550,7 @@ int fpt_cuda_trace_primary(const struct FptRenderConfig *config, const struct Fp
             !check(cudaMemsetAsync(c.counter, 0, 64, c.stream), "counter reset", error, error_len))
             return 1;
         skip.guard = c.counter + C_GUARD;
+        skip.cam_step = c.counter + C_CAMSTEP;
     }
     cudaEventRecord(c.ev0, c.stream);
     cudaError_t le = S.surrogate ? launch_skip_primary(S.kind, c.scene, S.width, S.height, skip, c.hits, c.stream)

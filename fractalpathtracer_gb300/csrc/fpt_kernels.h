@@ -32,8 +32,11 @@ struct KernelTimer {
 };
 
 // Bytes of wave scratch per path: path record (96), two march queues (8),
-// two shadow queues (128), shade queue (4).
-constexpr size_t kWaveBytesPerPath = 96 + 8 + 128 + 4;
+// two shadow queues (128), shade queue (4), surrogate-skip queue (32, at a
+// 16-byte aligned offset after the rest).
+constexpr size_t kWaveBytesPerPath = 96 + 8 + 128 + 4 + 32;
+inline size_t wave_scratch_bytes(size_t wave_paths) { return wave_paths * kWaveBytesPerPath + 16; }
+inline size_t wave_skip_offset(size_t wave_paths) { return (wave_paths * (96 + 8 + 128 + 4) + 15) & ~size_t(15); }
 
 struct PathLaunch {
     const DeviceScene *scene;   // device pointer
@@ -42,7 +45,7 @@ struct PathLaunch {
     uint32_t bounces;
     float4 *accum;              // width*height, running mean
     float4 *sample_rgb;         // width*height*(sample_end-sample_begin) scratch: one colour per path
-    void *wave_scratch;         // wave_paths * kWaveBytesPerPath bytes
+    void *wave_scratch;         // wave_scratch_bytes(wave_paths) bytes
     uint32_t wave_paths;        // paths per wave ("wavefront length")
     unsigned int *counters;     // 8 device words
     uint32_t sample_begin, sample_end;

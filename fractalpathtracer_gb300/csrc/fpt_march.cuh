@@ -53,6 +53,20 @@ __device__ __forceinline__ bool march_begin(March &m, const DeviceScene &S, floa
 
 __device__ __forceinline__ bool march_finish(March &m, bool found) { m.found = found; m.done = true; return false; }
 
+// Resumes the march of a ray from `start` that has taken `it` steps, the
+// last of length `step`, and stands at `pos`: the state march_update leaves
+// there (the step budget and the distance limit count from `start`, a
+// refinement starts from half of `step`).
+__device__ __forceinline__ bool march_resume(March &m, const DeviceScene &S, float3 start, float3 pos, float3 dir, int ni, float min_dist,
+                                             float lod_falloff, int it, float step) {
+    const bool more = march_begin(m, S, pos, dir, ni, min_dist, lod_falloff);
+    m.start = start;
+    m.it = it;
+    m.step = step;
+    if (more && m.it >= m.maxi) return march_finish(m, false);
+    return more;
+}
+
 // Mandelbulber refinement bracket: shaders/Shaders.metal:3733-3749.
 __device__ __forceinline__ bool mandel_refine_move(March &m) {
     if (m.dist < m.th && m.dist > m.th * m.limit) return march_finish(m, true);
@@ -207,6 +221,19 @@ __device__ March march_loop(const DeviceScene &S, float3 origin, float3 dir, int
     March m;
     TranslucencyProbe<KIND> probe{&S};
     bool more = march_begin(m, S, origin, dir, ni, min_dist, lod_falloff);
+    while (more) {
+        float d = scene_eval<KIND>(S, m.pos, EV_MAP).d;
+        more = march_update(m, S, d, probe);
+    }
+    return m;
+}
+// march_loop for a ray resumed at `pos` after `it` steps from `start` (march_resume).
+template <int KIND>
+__device__ March march_loop_from(const DeviceScene &S, float3 start, float3 pos, float3 dir, int ni, float min_dist, float lod_falloff,
+                                 int it, float step) {
+    March m;
+    TranslucencyProbe<KIND> probe{&S};
+    bool more = march_resume(m, S, start, pos, dir, ni, min_dist, lod_falloff, it, step);
     while (more) {
         float d = scene_eval<KIND>(S, m.pos, EV_MAP).d;
         more = march_update(m, S, d, probe);

@@ -95,6 +95,7 @@ struct DeviceScene {
     uint32_t fp64_bisection;
     uint32_t surrogate;
     float surrogate_margin, surrogate_safety;
+    uint32_t surrogate_max_iters;
     const void *surrogate_weights;  // device pointer to the packed MLP
 
     // --- HDRI LUT (reference world mode 2)

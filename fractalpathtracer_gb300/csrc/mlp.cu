@@ -453,10 +453,11 @@ bool surrogate_args(uint64_t model, const DeviceScene &S, unsigned long long *st
     for (int k = 0; k < 3; ++k) { A.lo[k] = hm->lo[k]; A.hi[k] = hm->hi[k]; }
     A.margin = S.surrogate_margin > 0.0f ? S.surrogate_margin : 0.1f;
     A.safety = S.surrogate_safety > 0.0f ? S.surrogate_safety : 0.9f;
-    A.max_iters = 64;
+    A.max_iters = S.surrogate_max_iters ? S.surrogate_max_iters : 64u;
     A.use_network = S.surrogate == FPT_CUDA_SURROGATE_SKIP ? 1u : 0u;
     A.engine = ctx().network_engine;
     A.guard = nullptr;
+    A.cam_step = nullptr;
     A.stats = stats;
     return true;
 }

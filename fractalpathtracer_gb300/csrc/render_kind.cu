@@ -16,7 +16,7 @@ cudaError_t launch_pathtrace_kind(const PathLaunch &pl, cudaStream_t stream, int
 
 template <int KIND>
 static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
-    WaveParams W;
+    WaveParams W{};
     W.scene = pl.scene;
     W.tiles_x = (pl.width + 7u) / 8u;
     const uint32_t tiles_y = (pl.height + 3u) / 4u;
@@ -32,6 +32,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         W.box_hi[k] = pl.skip ? pl.skip->hi[k] : 0.0f;
     }
     const bool skip_pass = pl.skip && pl.skip->use_network;
+    W.skip_queue = skip_pass ? 1u : 0u;
     W.ilv_batch = pl.ilv_batch;
     W.refill_batch = pl.refill_batch;
     // extension formulas can march with the orbit-interleaved kernel (schedule 1)
@@ -45,6 +46,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     W.q_march[0] = reinterpret_cast<uint32_t *>(base + size_t(cap) * (96 + 128));
     W.q_march[1] = W.q_march[0] + cap;
     W.q_shade = W.q_march[1] + cap;
+    W.q_skip = reinterpret_cast<SkipJob *>(base + wave_skip_offset(cap));
     int sms = 0, dev = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -90,6 +92,10 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         W.wave_base = uint32_t(wb);
         W.n_paths = uint32_t(std::min<uint64_t>(cap, total - wb));
         if ((e = cudaMemsetAsync(W.counters, 0, C_COUNT * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+        if (W.box_on && wb == 0) {
+            first_step_kernel<KIND><<<1, 32, 0, stream>>>(pl.scene, W.counters + C_CAMSTEP);
+            ++launches;
+        }
         camera_kernel<false><<<std::min<uint32_t>((W.n_paths + 255u) / 256u, uint32_t(sms) * 16u), 256, 0, stream>>>(W);
         ++launches;
         for (uint32_t b = 0; b <= pl.bounces; ++b) {
@@ -102,9 +108,9 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
             if (skip_pass && b == 0u)
                 timed(KC_SKIP, [&] {
                     if (skip_tc)
-                        skip_march_tc_kernel<KIND><<<skip_blocks, mlp::kTcRows, mlp::tc_smem_bytes(), stream>>>(W, cur, *pl.skip);
+                        skip_march_tc_kernel<KIND><<<skip_blocks, mlp::kTcRows, mlp::tc_smem_bytes(), stream>>>(W, *pl.skip);
                     else
-                        skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, cur, *pl.skip);
+                        skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, *pl.skip);
                 });
             timed(KC_MARCH, [&] {
                 if (interleaved) march_ilv_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
@@ -164,6 +170,7 @@ cudaError_t FPT_CAT(launch_skip_primary_k, FPT_KIND)(const DeviceScene *scene, u
         cudaFuncSetAttribute(skip_primary_tc_kernel<FPT_KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mlp::tc_smem_bytes()));
         attr = true;
     }
+    if (args.cam_step) first_step_kernel<FPT_KIND><<<1, 32, 0, st>>>(scene, const_cast<uint32_t *>(args.cam_step));
     if (args.engine == kNetTcgen05) {
         const uint32_t blocks = (W * H + uint32_t(mlp::kTcRows) - 1u) / uint32_t(mlp::kTcRows);
         skip_primary_tc_kernel<FPT_KIND><<<blocks, mlp::kTcRows, mlp::tc_smem_bytes(), st>>>(scene, args, hits);

@@ -38,6 +38,7 @@ struct SkipArgs {
     uint32_t use_network;        // 0: box clip only (the march kernel applies it; no skip pass)
     uint32_t engine;             // network engine: kNetTcgen05 or kNetMmaSync
     uint32_t *guard;             // primary-ray pass: error word (bit 2: an MMA did not complete), or null
+    const uint32_t *cam_step;    // primary-ray pass: the plain march's first step from the camera (float bits), or null
     unsigned long long *stats;   // kSkipStats counters or null
 };
 
@@ -71,17 +72,25 @@ enum SkipPhase : int { SP_IDLE = 0, SP_EXACT = 1, SP_PROPOSE = 2 };
 
 struct SkipLane {
     float3 origin, dir;   // job start and direction
-    float t;              // advance along dir from origin
+    float3 pos;           // position, advanced step by step like the exact march's (pos + dir * step)
+    float t;              // advance along dir from origin (box exit test)
     float t_exit;         // box exit (advance)
-    float d;              // exact distance at origin + t dir (SP_PROPOSE)
+    float d;              // exact distance at pos (SP_PROPOSE)
     float lam;            // look-ahead in units of d
     int phase;
     uint32_t iters;
+    int steps;            // march steps from the ray's origin (plain steps and accepted skips)
+    float last_step;      // length of the last of them
 };
 
 // Starts a lane on a ray: clips to the box.  Returns false when the ray
 // never meets the box (a miss; t is left at 0).
-__device__ __forceinline__ bool skip_begin(SkipLane &L, const SkipArgs &A, float3 origin, float3 dir) {
+// t_start >= 0: the ray starts there (before the box too); t_start < 0: at
+// the box entry.
+// `steps` / `last_step`: plain-march steps already taken to reach origin +
+// t_start dir.
+__device__ __forceinline__ bool skip_begin(SkipLane &L, const SkipArgs &A, float3 origin, float3 dir, float t_start, int steps,
+                                           float last_step) {
     L.origin = origin;
     L.dir = dir;
     L.t = 0.0f;
@@ -90,20 +99,45 @@ __device__ __forceinline__ bool skip_begin(SkipLane &L, const SkipArgs &A, float
     L.lam = 2.0f;
     float tn, tf;
     if (!box_span(A, origin, dir, tn, tf)) { L.phase = SP_IDLE; return false; }
+    if (t_start >= 0.0f) tn = t_start;
+    if (tn > tf) { L.phase = SP_IDLE; return false; }
     L.t = tn;
+    L.pos = tn > 0.0f ? origin + dir * tn : origin;
+    L.steps = steps;
+    L.last_step = last_step;
     L.t_exit = tf;
     L.phase = SP_EXACT;
     return true;
 }
 
+// Start of a primary ray in the primary-ray pass: the plain march's first
+// step from the camera when there is one (see first_step_kernel), else the
+// box entry.
+__device__ __forceinline__ float first_step_or_entry(const SkipArgs &A) {
+    const float s1 = A.cam_step ? bitsf(*A.cam_step) : 0.0f;
+    return s1 > 0.0f ? s1 : -1.0f;
+}
+
 enum SkipOutcome : int { SO_CONTINUE = 0, SO_HANDOVER = 1, SO_ESCAPE = 2 };
+
+// One step of the scene's march rule (march_update) from the lane's position
+// with its exact distance L.d, applied to the position the way the exact
+// march applies it, so steps the network does not replace visit the plain
+// march's positions.
+__device__ __forceinline__ void plain_advance(SkipLane &L, const DeviceScene &S) {
+    const float step = S.sdf_id == FPT_SDF_MANDELBULBER ? mandel_march_step(L.d, mandel_threshold(L.pos, S), S) : fabsf(L.d) * 0.99f;
+    L.pos = L.pos + L.dir * step;
+    L.t += step;
+    ++L.steps;
+    L.last_step = step;
+}
 
 // The network query of a lane in SP_PROPOSE: the look-ahead point p + lam d
 // dir, normalised to the model box (other lanes query their position; the
 // row is computed but not used).  Returns whether the lane proposes.
 __device__ __forceinline__ bool skip_query(const SkipLane &L, const SkipArgs &A, float u[3]) {
     const bool propose = A.use_network && L.phase == SP_PROPOSE;
-    const float3 p = L.origin + L.dir * L.t;
+    const float3 p = L.pos;
     const float3 q0 = propose ? p + L.dir * (L.lam * L.d) : p;
     u[0] = (q0.x - A.M.center[0]) * A.M.inv_half[0];
     u[1] = (q0.y - A.M.center[1]) * A.M.inv_half[1];
@@ -127,24 +161,27 @@ __device__ __forceinline__ int skip_advance(SkipLane &L, const DeviceScene &S, c
         if (s > 1.25f * L.d && isfinite(s)) {
             cand = true;
         } else {   // no useful proposal: the plain step
-            L.t += 0.99f * L.d;
+            plain_advance(L, S);
             L.phase = SP_EXACT;
         }
     } else if (L.phase == SP_PROPOSE) {   // box-only mode: plain steps
-        L.t += 0.99f * L.d;
+        plain_advance(L, S);
     }
-    const float3 e_pt = L.origin + L.dir * (cand ? L.t + s : L.t);
-    const float de = scene_eval<KIND>(S, e_pt, EV_MAP).d;
+    const float3 q = L.pos + L.dir * s;
+    const float de = scene_eval<KIND>(S, cand ? q : L.pos, EV_MAP).d;
     ++c_exact;
     if (cand) {
         if (s <= L.d + de && isfinite(de)) {
             L.lam = fminf(fmaxf(1.5f * s / L.d, 2.0f), 32.0f);
+            L.pos = q;
             L.t += s;
+            ++L.steps;
+            L.last_step = s;
             L.d = de;
             ++c_acc;
         } else {
             L.lam = 2.0f;
-            L.t += 0.99f * L.d;
+            plain_advance(L, S);
             L.phase = SP_EXACT;
             ++c_rej;
         }
@@ -190,90 +227,66 @@ __device__ __forceinline__ void skip_flush_stats(const SkipArgs &A, int lane, ui
     }
 }
 
-// Takes jobs for the warp's idle lanes (warp-synchronous: one atomic per warp
-// per try).  Rays that miss the box are resolved at once and the lane draws
-// again.
-__device__ __forceinline__ void skip_refill(SkipLane &L, const SkipArgs &A, const WaveParams &W, int cur, uint32_t n_path,
-                                            uint32_t total, int lane, bool &retired, uint32_t &job, bool &shadow, uint32_t &c_esc) {
+// Takes jobs for the warp's idle lanes from the skip queue (camera rays that
+// enter the box, queued by the camera kernel): warp-synchronous, one atomic
+// per warp.
+__device__ __forceinline__ void skip_refill(SkipLane &L, const SkipArgs &A, const WaveParams &W, uint32_t total, int lane,
+                                            bool &retired, uint32_t &job, uint32_t &c_esc) {
     const unsigned FULL = 0xffffffffu;
-    for (int tries = 0; tries < 4; ++tries) {
-        const bool need = L.phase == SP_IDLE && !retired;
-        unsigned ballot = __ballot_sync(FULL, need);
-        if (!ballot) break;
-        uint32_t leader = __ffs(ballot) - 1, base = 0;
-        if (lane == int(leader)) base = atomicAdd(&W.counters[C_SKIP], (unsigned)__popc(ballot));
-        base = __shfl_sync(FULL, base, leader);
-        if (need) {
-            uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
-            if (idx >= total) {
-                retired = true;
-            } else {
-                shadow = idx >= n_path;
-                float3 o, d;
-                if (!shadow) {
-                    job = W.q_march[cur][idx];
-                    const PathRec &R = W.paths[job];
-                    o = mk3(R.pos.x, R.pos.y, R.pos.z);
-                    d = mk3(R.dir.x, R.dir.y, R.dir.z);
-                } else {
-                    job = idx - n_path;
-                    const ShadowJob &J = W.q_shadow[cur][job];
-                    o = mk3(J.origin.x, J.origin.y, J.origin.z) + mk3(J.normal.x, J.normal.y, J.normal.z) * 0.001f;
-                    d = mk3(J.dir.x, J.dir.y, J.dir.z);
-                }
-                if (!skip_begin(L, A, o, d)) {
-                    ++c_esc;
-                    if (!shadow) W.paths[job].color.w = bitsf(fbits(W.paths[job].color.w) | PF_ESCAPED);
-                    else W.q_shadow[cur][job].dir.w = 1.0f;
-                }
-            }
-        }
+    const bool need = L.phase == SP_IDLE && !retired;
+    const unsigned ballot = __ballot_sync(FULL, need);
+    if (!ballot) return;
+    const uint32_t leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if (lane == int(leader)) base = atomicAdd(&W.counters[C_SKIP], (unsigned)__popc(ballot));
+    base = __shfl_sync(FULL, base, leader);
+    if (!need) return;
+    const uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
+    if (idx >= total) {
+        retired = true;
+        return;
+    }
+    const float4 o = W.q_skip[idx].origin, d = W.q_skip[idx].dir;
+    job = fbits(o.w);
+    if (!skip_begin(L, A, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, int(d.w), 0.0f)) {   // only where the camera kernel's start lies on the box exit
+        ++c_esc;
+        W.paths[job].color.w = bitsf(fbits(W.paths[job].color.w) | PF_ESCAPED);
     }
 }
 
-// Writes the outcome of a lane whose skip ended (escape or hand-over) and
-// idles the lane.
-__device__ __forceinline__ void skip_finish(SkipLane &L, const WaveParams &W, int cur, int out, uint32_t job, bool shadow,
-                                            uint32_t &c_esc, uint32_t &c_hand) {
+// Writes the outcome of a lane whose skip ended (escape or hand-over) into
+// its path record and idles the lane.
+__device__ __forceinline__ void skip_finish(SkipLane &L, const WaveParams &W, int out, uint32_t job, uint32_t &c_esc, uint32_t &c_hand) {
     if (out == SO_ESCAPE) ++c_esc; else ++c_hand;
     const bool known = out == SO_HANDOVER && L.phase == SP_PROPOSE;   // L.d is the exact distance here
-    if (!shadow) {
-        PathRec &R = W.paths[job];
-        float3 p = L.origin + L.dir * L.t;
-        R.pos = make_float4(p.x, p.y, p.z, R.pos.w);
-        if (out == SO_ESCAPE) R.color.w = bitsf(fbits(R.color.w) | PF_ESCAPED);
-        if (known) {
-            R.grad.w = L.d;
-            R.color.w = bitsf(fbits(R.color.w) | PF_KNOWN_D);
-        }
-    } else {
-        ShadowJob &J = W.q_shadow[cur][job];
-        J.normal.w = L.t;
-        if (out == SO_ESCAPE) J.dir.w = 1.0f;
-        if (known) {
-            J.contrib.w = L.d;
-            J.dir.w = 2.0f;
-        }
+    PathRec &R = W.paths[job];
+    const float3 p = L.pos;
+    R.pos = make_float4(p.x, p.y, p.z, R.pos.w);
+    R.shadow.w = float(L.steps);
+    uint32_t st = fbits(R.color.w);
+    if (out == SO_ESCAPE) st |= PF_ESCAPED;
+    if (known) {
+        R.grad.w = L.d;
+        st |= PF_KNOWN_D;
     }
+    R.color.w = bitsf(st);
     L.phase = SP_IDLE;
 }
 
-// Wavefront pass: advances the path rays of q_march[cur] and the shadow
-// rays of q_shadow[cur] before the exact march kernel takes them.  Path rays
-// move R.pos; escapes set PF_ESCAPED (the march kernel then classifies them
-// as misses without evaluating).  Shadow rays keep their advance in
-// normal.w; escapes set dir.w = 1 (unoccluded).  Jobs are taken with
-// per-lane regeneration from counter C_SKIP.  Network on mma.sync, one warp
-// (32 rows) at a time.
+// Wavefront pass before the first march pass: advances the camera rays of
+// the skip queue before the exact march kernel takes them.  A ray's R.pos
+// moves; an escape sets PF_ESCAPED (the march kernel then classifies the ray
+// as a miss without evaluating); a hand-over with the exact distance in hand
+// sets PF_KNOWN_D.  Jobs are taken with per-lane regeneration from counter
+// C_SKIP.  Network on mma.sync, one warp (32 rows) at a time.
 template <int KIND>
-__global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WaveParams W, int cur, SkipArgs A) {
+__global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WaveParams W, SkipArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::SmemWeights &sw = *reinterpret_cast<mlp::SmemWeights *>(smem_raw);
     mlp::WarpForward *wf_all =
         reinterpret_cast<mlp::WarpForward *>(smem_raw + ((sizeof(mlp::SmemWeights) + 127) & ~size_t(127)));
     const DeviceScene &S = *W.scene;
-    const uint32_t n_path = W.counters[C_MARCH0 + cur];
-    const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
+    const uint32_t total = W.counters[C_SKIPN];
     if (total == 0u) return;
     mlp::load_weights(sw, A.M);
     __syncthreads();
@@ -284,21 +297,55 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WavePara
     L.phase = SP_IDLE;
     bool retired = false;
     uint32_t job = 0;
-    bool shadow = false;
     uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
     uint32_t trips = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
         if (loop_guard(trips, t0, W.counters)) break;
-        skip_refill(L, A, W, cur, n_path, total, lane, retired, job, shadow, c_esc);
+        skip_refill(L, A, W, total, lane, retired, job, c_esc);
         if (!__any_sync(FULL, L.phase != SP_IDLE)) {
             if (__all_sync(FULL, retired)) break;
             continue;
         }
         const int out = skip_step<KIND>(L, S, A, sw, wf, lane, c_rows, c_fwd, c_exact, c_acc, c_rej);
-        if (L.phase != SP_IDLE && out != SO_CONTINUE) skip_finish(L, W, cur, out, job, shadow, c_esc, c_hand);
+        if (L.phase != SP_IDLE && out != SO_CONTINUE) skip_finish(L, W, out, job, c_esc, c_hand);
     }
     skip_flush_stats(A, lane, c_rows, c_fwd, c_exact, c_acc, c_rej, c_esc, c_hand);
+}
+
+// Job feed of the CTA-synchronous pass.  A stall of one warp stalls the
+// whole CTA there, so refills must not wait on memory: each warp takes job
+// indices from a chunk it claimed one chunk ahead (the claim's atomic result
+// is read only when the current chunk runs out), and each lane loads its next
+// job one job ahead (the loads are consumed when the lane's current ray ends).
+constexpr uint32_t kSkipChunk = 64;
+struct SkipFeed {
+    uint32_t cur_base, taken, next_base;   // the same in every lane of the warp
+    uint32_t pending;                      // lane 0: claim of the chunk after next (read at the next roll-over)
+};
+__device__ __forceinline__ void feed_init(SkipFeed &F, const WaveParams &W, int lane) {
+    uint32_t a = 0;
+    if (lane == 0) a = atomicAdd(&W.counters[C_SKIP], 2u * kSkipChunk);
+    a = __shfl_sync(0xffffffffu, a, 0);
+    F.cur_base = a;
+    F.next_base = a + kSkipChunk;
+    F.taken = 0;
+    F.pending = 0;
+    if (lane == 0) F.pending = atomicAdd(&W.counters[C_SKIP], kSkipChunk);
+}
+// The next job index of every lane with `need` (warp-synchronous).
+__device__ __forceinline__ uint32_t feed_take(SkipFeed &F, bool need, const WaveParams &W, int lane) {
+    const unsigned ballot = __ballot_sync(0xffffffffu, need);
+    const uint32_t pos = F.taken + __popc(ballot & ((1u << lane) - 1u));
+    const uint32_t idx = pos < kSkipChunk ? F.cur_base + pos : F.next_base + (pos - kSkipChunk);
+    F.taken += __popc(ballot);
+    if (F.taken >= kSkipChunk) {   // at most 32 indices spill into the next chunk
+        F.taken -= kSkipChunk;
+        F.cur_base = F.next_base;
+        F.next_base = __shfl_sync(0xffffffffu, F.pending, 0);
+        if (lane == 0) F.pending = atomicAdd(&W.counters[C_SKIP], kSkipChunk);
+    }
+    return idx;
 }
 
 // The same pass with the network on the 5th-generation tensor cores: the
@@ -306,20 +353,22 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WavePara
 // 128-thread CTA proposes runs one 128-row forward pass (mlp::tc_forward).
 // Guard word bits: 1 = loop time limit, 2 = an MMA did not complete.
 template <int KIND>
-__global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WaveParams W, int cur, SkipArgs A) {
+__global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WaveParams W, SkipArgs A) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
     const DeviceScene &S = *W.scene;
-    const uint32_t n_path = W.counters[C_MARCH0 + cur];
-    const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
+    const uint32_t total = W.counters[C_SKIPN];
     if (total == 0u) return;
     mlp::tc_setup(sm, A.M);
     const int lane = threadIdx.x & 31;
     SkipLane L;
     L.phase = SP_IDLE;
-    bool retired = false, shadow = false, fail = false;
+    bool fed_out = false, has_next = false, fail = false;
+    float4 next_o = make_float4(0.f, 0.f, 0.f, 0.f), next_d = next_o;
     uint32_t job = 0, phase = 0;
     uint32_t c_rows = 0, c_fwd = 0, c_exact = 0, c_acc = 0, c_rej = 0, c_esc = 0, c_hand = 0;
+    SkipFeed F;
+    feed_init(F, W, lane);
     uint32_t trips = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
@@ -329,7 +378,29 @@ __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WavePara
                 break;
             }
         }
-        skip_refill(L, A, W, cur, n_path, total, lane, retired, job, shadow, c_esc);
+        // An idle lane starts the job it loaded earlier, then loads its next one.
+        if (L.phase == SP_IDLE && has_next) {
+            has_next = false;
+            job = fbits(next_o.w);
+            if (!skip_begin(L, A, mk3(next_o.x, next_o.y, next_o.z), mk3(next_d.x, next_d.y, next_d.z), 0.0f, int(next_d.w), 0.0f)) {
+                ++c_esc;   // only where the camera kernel's start lies on the box exit
+                W.paths[job].color.w = bitsf(fbits(W.paths[job].color.w) | PF_ESCAPED);
+            }
+        }
+        {
+            const bool want = !has_next && !fed_out;
+            const uint32_t idx = feed_take(F, want, W, lane);
+            if (want) {
+                if (idx < total) {
+                    next_o = W.q_skip[idx].origin;
+                    next_d = W.q_skip[idx].dir;
+                    has_next = true;
+                } else {
+                    fed_out = true;
+                }
+            }
+        }
+        const bool retired = L.phase == SP_IDLE && !has_next && fed_out;
         if (!__syncthreads_or(L.phase != SP_IDLE)) {
             if (__syncthreads_and(retired)) break;
             continue;
@@ -344,7 +415,7 @@ __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WavePara
             if (propose) ++c_rows;
         }
         const int out = skip_advance<KIND>(L, S, A, propose, m, c_exact, c_acc, c_rej);
-        if (L.phase != SP_IDLE && out != SO_CONTINUE) skip_finish(L, W, cur, out, job, shadow, c_esc, c_hand);
+        if (L.phase != SP_IDLE && out != SO_CONTINUE) skip_finish(L, W, out, job, c_esc, c_hand);
     }
     mlp::tc_teardown(sm);
     if (fail && threadIdx.x == 0) atomicOr(W.counters + C_GUARD, 2u);
@@ -381,7 +452,8 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_primary_kernel(const 
         L.phase = SP_IDLE;
         bool escaped = false;
         uint32_t exact0 = c_exact;
-        if (ray && !skip_begin(L, A, rp, dr)) escaped = true;
+        const float t_start = first_step_or_entry(A);
+        if (ray && !skip_begin(L, A, rp, dr, t_start, t_start > 0.0f ? 1 : 0, fmaxf(t_start, 0.0f))) escaped = true;
         while (__any_sync(0xffffffffu, L.phase != SP_IDLE)) {
             int out = skip_step<KIND>(L, S, A, sw, wf, lane, c_rows, c_fwd, c_exact, c_acc, c_rej);
             if (L.phase != SP_IDLE && out != SO_CONTINUE) {
@@ -397,8 +469,7 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_primary_kernel(const 
                 h.distance = S.render[4];
                 h.steps = c_exact - exact0;
             } else {
-                float3 start = L.origin + L.dir * L.t;
-                March m = march_loop<KIND>(S, start, dr, int(S.render[1]), S.render[3], 0.0002f);
+                March m = march_loop_from<KIND>(S, rp, L.pos, dr, int(S.render[1]), S.render[3], 0.0002f, L.steps, L.last_step);
                 float travel = len3(m.pos - rp);
                 bool hit = m.found && isfinite(travel) && travel < S.render[4] * 0.99f;
                 h.distance = travel;
@@ -442,7 +513,8 @@ __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_primary_tc_kernel(const 
         L.phase = SP_IDLE;
         bool escaped = false;
         uint32_t exact0 = c_exact;
-        if (ray && !skip_begin(L, A, rp, dr)) escaped = true;
+        const float t_start = first_step_or_entry(A);
+        if (ray && !skip_begin(L, A, rp, dr, t_start, t_start > 0.0f ? 1 : 0, fmaxf(t_start, 0.0f))) escaped = true;
         while (__syncthreads_or(L.phase != SP_IDLE)) {
             float u[3];
             const bool propose = skip_query(L, A, u);
@@ -468,8 +540,7 @@ __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_primary_tc_kernel(const 
                 h.distance = S.render[4];
                 h.steps = c_exact - exact0;
             } else {
-                float3 start = L.origin + L.dir * L.t;
-                March m = march_loop<KIND>(S, start, dr, int(S.render[1]), S.render[3], 0.0002f);
+                March m = march_loop_from<KIND>(S, rp, L.pos, dr, int(S.render[1]), S.render[3], 0.0002f, L.steps, L.last_step);
                 float travel = len3(m.pos - rp);
                 bool hit = m.found && isfinite(travel) && travel < S.render[4] * 0.99f;
                 h.distance = travel;

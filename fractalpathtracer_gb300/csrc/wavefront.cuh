@@ -40,8 +40,15 @@ struct alignas(16) PathRec {
     float4 dir;     // xyz direction, w sky mask
     float4 color;   // xyz throughput, w state bits (bounce | flags)
     float4 light;   // xyz emission + environment light, w slot bits
-    float4 shadow;  // xyz sun light from shadow rays
+    float4 shadow;  // xyz sun light from shadow rays, w plain-march steps a camera ray took before the march kernel
     float4 grad;    // xyz background gradient colour of the camera ray, w exact distance (PF_KNOWN_D)
+};
+
+// A camera ray that enters the surrogate's box, queued by the camera kernel
+// for the skip pass.
+struct alignas(16) SkipJob {
+    float4 origin;  // xyz march start of the camera ray, w path index bits
+    float4 dir;     // xyz direction, w plain-march steps already taken (0 or 1)
 };
 
 struct alignas(16) ShadowJob {
@@ -53,10 +60,14 @@ struct alignas(16) ShadowJob {
 };
 
 // Device counters of one wave.
-enum Counter : uint32_t { C_MARCH0 = 0, C_MARCH1 = 1, C_SHADOW0 = 2, C_SHADOW1 = 3, C_SHADE = 4, C_HEAD = 5, C_SKIP = 6, C_COUNT = 8 };
+enum Counter : uint32_t { C_MARCH0 = 0, C_MARCH1 = 1, C_SHADOW0 = 2, C_SHADOW1 = 3, C_SHADE = 4, C_HEAD = 5, C_SKIP = 6, C_SKIPN = 7,
+                          C_COUNT = 8 };
 // Word after the wave counters (not cleared between waves): set when a
 // persistent loop ran past its time limit and gave up (the host reports it).
 constexpr uint32_t C_GUARD = 8;
+// Word holding the plain march's first step from a pinhole camera (float
+// bits; written by first_step_kernel, read by the camera kernel).
+constexpr uint32_t C_CAMSTEP = 9;
 // Lockstep march: finished lanes write their results and take new rays in
 // groups of this many (measured at 1080p 16 spp: 2 -> 863, 4 -> 923, 8 -> 944,
 // 16 -> 903 Mpaths/s, against 797 when every lane refills at once).
@@ -96,6 +107,10 @@ struct WaveParams {
     // ray enters the box and ends as a miss where it leaves it.
     uint32_t box_on;
     float box_lo[3], box_hi[3];
+    // Surrogate-skip pass: the camera kernel flags camera rays that miss the
+    // box as escaped and queues the others here (count in C_SKIPN).
+    uint32_t skip_queue;
+    SkipJob *q_skip;
     // Batched scenes (multi-scene passes, one sample per pass; null otherwise).
     // A path's scene is bits 16..31 of its state word.
     const DeviceScene *scenes;
@@ -173,6 +188,38 @@ __device__ __forceinline__ PathRng path_rng(const DeviceScene &S, uint32_t pixel
 }
 
 // ---------------------------------------------------------------- camera
+// The plain march's first step from a pinhole camera.  Every camera ray
+// starts at the camera, so its first distance evaluation is the same for all
+// of them.  With the box clip, camera rays start at this step: the clipped
+// march then visits the plain march's positions, and the box only decides
+// misses (rays that never meet it, or whose first step passes it) and exits.
+// (A start at the box entry instead changes the positions the march visits,
+// and where the distance estimate exceeds the true distance, as the
+// Mandelbox's does seen from outside, the plain march's steps pass over
+// surface that a march from the box entry finds.)  0 when the camera has a
+// lens (origins differ) or the plain march ends at the camera; camera rays
+// then start at the box entry.
+template <int KIND>
+__global__ void first_step_kernel(const DeviceScene *scene, uint32_t *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const DeviceScene &S = *scene;
+    float s1 = 0.0f;
+    if (!(S.camera_dof > 0.0f)) {
+        const float3 cam = mk3(S.cam_pos[0], S.cam_pos[1], S.cam_pos[2]);
+        const float d = scene_eval<KIND>(S, cam, EV_MAP).d;
+        if (isfinite(d)) {
+            if (S.sdf_id == FPT_SDF_MANDELBULBER) {   // march_update, Mandelbulber branch
+                const float th = mandel_threshold(cam, S);
+                if (!(d < th)) s1 = mandel_march_step(d, th, S);
+            } else {                                  // march_update, FPT rule (lod = min_dist at the start)
+                const float o = fabsf(d) * 0.99f;
+                if (!(o < S.render[3]) && !(S.render[4] < o)) s1 = o;
+            }
+        }
+    }
+    *out = fbits(s1);
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p - threadIdx.x < W.n_paths; p += gridDim.x * blockDim.x) {
@@ -195,14 +242,15 @@ __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
             }
         }
         const DeviceScene &S = *sp;
-        bool march = false;
+        bool march = false, skip = false;
+        float3 rp = mk3(0.0f), dr = mk3(0.0f, 0.0f, 1.0f);
+        float steps0 = 0.0f;   // plain-march steps taken by the start (the skip queue's dir.w)
         if (valid) {
             uint32_t pixel = py * S.width + px;
             uint32_t sample = BATCH ? *W.pass : W.sample_begin + s_rel;
             float2 uv = screen_uv(px, py, S);
             PathRng rng;
             rng.init(S.rng == FPT_CUDA_RNG_PCG, S.seed, pixel, sample, uv.x, uv.y);
-            float3 rp, dr;
             PathRec R;
             uint32_t slot = BATCH ? W.pixel_base[k] + pixel : pixel * W.sample_count + s_rel;
             R.light = make_float4(0.f, 0.f, 0.f, bitsf(slot));
@@ -220,6 +268,26 @@ __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
                 float3 g = background_gradient(dr, S);
                 R.grad = make_float4(g.x, g.y, g.z, 0.f);
                 march = !done;
+                if (march && W.box_on) {   // start at the plain march's first step (else the box entry)
+                    float tn, tf;
+                    if (!wave_box_span(W, rp, dr, tn, tf)) {
+                        R.color.w = bitsf(fbits(R.color.w) | PF_ESCAPED);
+                    } else {
+                        const float s1 = bitsf(W.counters[C_CAMSTEP]);
+                        const float t0 = s1 > 0.0f ? s1 : tn;
+                        if (t0 > tf) {   // the plain march's first step passes the whole box
+                            R.color.w = bitsf(fbits(R.color.w) | PF_ESCAPED);
+                        } else {
+                            if (t0 > 0.0f) {
+                                rp = rp + dr * t0;
+                                R.pos = make_float4(rp.x, rp.y, rp.z, 1.0f);
+                            }
+                            steps0 = s1 > 0.0f ? 1.0f : 0.0f;   // the plain march's first step is taken
+                            R.shadow.w = steps0;
+                            skip = W.skip_queue != 0u;
+                        }
+                    }
+                }
             }
             W.paths[p] = R;
         } else if (in_wave) {
@@ -227,6 +295,11 @@ __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
         }
         uint32_t at = warp_append(&W.counters[C_MARCH0], march);
         if (march) W.q_march[0][at] = p;
+        uint32_t sat = warp_append(&W.counters[C_SKIPN], skip);
+        if (skip) {
+            W.q_skip[sat].origin = make_float4(rp.x, rp.y, rp.z, bitsf(p));
+            W.q_skip[sat].dir = make_float4(dr.x, dr.y, dr.z, steps0);
+        }
     }
 }
 
@@ -293,9 +366,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
                         m.pos = o + dv * (S.render[4] + len3(o - cam) + 1.0f);
                     } else {
                         box_origin = o;
-                        box_exit = tf;
-                        active = march_begin(m, S, o + dv * tn, dv, ni, S.render[3], 0.0002f);
-                        have_d = active && (st & PF_KNOWN_D) && tn == 0.0f;
+                        // Leaving the box ends camera rays as misses (their march would end beyond the far limit from
+                        // the camera).  Later path rays keep marching: the reference counts a bounce whose march stops
+                        // within the far limit of the camera as a hit (shaders/Shaders.metal:5971-5976), wherever it
+                        // stops, and the box must not change that.
+                        box_exit = job.bounce == 0u ? tf : 3.0e38f;
+                        // the camera kernel (or the skip pass) placed camera rays; later rays start inside the box
+                        const int before = job.bounce == 0u ? int(R.shadow.w) : 0;
+                        if (before > 0)   // resumes the plain march from the camera (first step s1, or the skip pass's)
+                            active = march_resume(m, S, cam, o, dv, ni, S.render[3], 0.0002f, before,
+                                                  before == 1 ? bitsf(W.counters[C_CAMSTEP]) : 0.0f);
+                        else
+                            active = march_begin(m, S, o, dv, ni, S.render[3], 0.0002f);
+                        have_d = active && (st & PF_KNOWN_D);
                         known_d = R.grad.w;
                     }
                     pending = !active;
@@ -322,8 +405,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
                     } else {
                         box_origin = start;
                         box_exit = tf;
-                        active = march_begin(m, S, start + dv * tn, dv, int(S.render[1]), S.render[3], 0.0002f);
-                        have_d = active && d.w == 2.0f && tn == 0.0f;
+                        active = march_begin(m, S, start, dv, int(S.render[1]), S.render[3], 0.0002f);
+                        have_d = active && d.w == 2.0f;
                         known_d = J.contrib.w;
                     }
                     pending = !active;
@@ -468,9 +551,19 @@ __global__ void __launch_bounds__(128, 7) march_ilv_kernel(WaveParams W, int cur
                         m.pos = o + dv * (S.render[4] + len3(o - cam) + 1.0f);
                     } else {
                         box_origin = o;
-                        box_exit = tf;
-                        active = march_begin(m, S, o + dv * tn, dv, ni, S.render[3], 0.0002f);
-                        have_d = active && (st & PF_KNOWN_D) && tn == 0.0f;
+                        // Leaving the box ends camera rays as misses (their march would end beyond the far limit from
+                        // the camera).  Later path rays keep marching: the reference counts a bounce whose march stops
+                        // within the far limit of the camera as a hit (shaders/Shaders.metal:5971-5976), wherever it
+                        // stops, and the box must not change that.
+                        box_exit = job.bounce == 0u ? tf : 3.0e38f;
+                        // the camera kernel (or the skip pass) placed camera rays; later rays start inside the box
+                        const int before = job.bounce == 0u ? int(R.shadow.w) : 0;
+                        if (before > 0)   // resumes the plain march from the camera (first step s1, or the skip pass's)
+                            active = march_resume(m, S, cam, o, dv, ni, S.render[3], 0.0002f, before,
+                                                  before == 1 ? bitsf(W.counters[C_CAMSTEP]) : 0.0f);
+                        else
+                            active = march_begin(m, S, o, dv, ni, S.render[3], 0.0002f);
+                        have_d = active && (st & PF_KNOWN_D);
                         known_d = R.grad.w;
                     }
                     pending = !active;
@@ -492,8 +585,8 @@ __global__ void __launch_bounds__(128, 7) march_ilv_kernel(WaveParams W, int cur
                     } else {
                         box_origin = start;
                         box_exit = tf;
-                        active = march_begin(m, S, start + dv * tn, dv, int(S.render[1]), S.render[3], 0.0002f);
-                        have_d = active && d.w == 2.0f && tn == 0.0f;
+                        active = march_begin(m, S, start, dv, int(S.render[1]), S.render[3], 0.0002f);
+                        have_d = active && d.w == 2.0f;
                         known_d = J.contrib.w;
                     }
                     pending = !active;

@@ -203,7 +203,7 @@ class FptCudaSceneExt(C.Structure):
         ("sky_height", C.c_uint32), ("sky_rgb", C.POINTER(C.c_float)), ("sun_direction", C.c_float * 3),
         ("sun_intensity", C.c_float), ("fp64_bisection", C.c_uint32), ("surrogate", C.c_uint32),
         ("surrogate_model", C.c_uint64), ("surrogate_margin", C.c_float), ("surrogate_safety", C.c_float),
-        ("_reserved", C.c_uint32 * 8),
+        ("surrogate_max_iters", C.c_uint32), ("_reserved", C.c_uint32 * 7),
     ]
 
 

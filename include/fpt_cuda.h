@@ -598,7 +598,8 @@ struct FptCudaSceneExt {
     uint64_t surrogate_model;    /* handle from fpt_cuda_mlp_create */
     float surrogate_margin;      /* exact-DE hand-over distance for surrogate skips (0: 0.1) */
     float surrogate_safety;      /* step = safety * surrogate distance */
-    uint32_t _reserved[8];
+    uint32_t surrogate_max_iters;/* skip iterations per ray before the exact march takes over (0: 64) */
+    uint32_t _reserved[7];
 };
 
 /* Per-primary-ray output of fpt_cuda_trace_primary. */

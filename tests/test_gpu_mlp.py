@@ -198,3 +198,33 @@ def test_skip_render_matches_plain(trained_bulb, native):
     print("skip vs plain render:", m, st)
     assert st["accepted"] > 0 and st["escaped"] > 0
     assert m["mae"] <= 2.0 and m["lf_ssim"] >= 0.98, m
+
+
+def test_mandelbox_skip(native):
+    """The learned skip on the second surrogate scene, the scale -1.5 Mandelbox: a model trained on its own
+    DE; primary-ray hits equal to the plain march's and a render equal to the plain render within noise."""
+    import ctypes
+    b = scenes.mandelbox_path(256, 144, 8, 4)
+    lo, hi = scenes.SURROGATE_BOXES["mandelbox"]
+    h, stats = nx.mlp_create(b.cfg, b.ext, nx.mlp_config(lo, hi, points=1 << 20, steps=800, batch=8192, lr=2e-3, seed=4))
+    try:
+        assert stats["loss_last"] < 0.1 * stats["loss_first"], stats
+        e = type(b.ext)()
+        ctypes.memmove(ctypes.byref(e), ctypes.byref(b.ext), ctypes.sizeof(b.ext))
+        e.surrogate, e.surrogate_model = 1, h
+        hp, _ = native.trace_primary(b.cfg, b.ext)
+        hs, _ = native.trace_primary(b.cfg, e)
+        st_primary = nx.skip_stats()
+        agree = ((hp["hit"] > 0) == (hs["hit"] > 0)).mean()
+        both = (hp["hit"] > 0) & (hs["hit"] > 0)
+        dt = np.abs(hp["distance"][both].astype(np.float64) - hs["distance"][both]) / (1.0 + hp["distance"][both])
+        print(f"mandelbox primary: agree {agree:.5f} p99 rel dist delta {np.percentile(dt, 99):.2e}", st_primary)
+        assert agree >= 0.995 and np.percentile(dt, 99) <= 5e-5
+        assert st_primary["accepted"] > 0
+        _, rgba_p, _ = native.cuda_render(b.cfg, b.ext, linear=False)
+        _, rgba_s, _ = native.cuda_render(b.cfg, e, linear=False)
+        m = oracle.image_metrics(rgba_p, rgba_s)
+        print("mandelbox skip vs plain render:", m, nx.skip_stats())
+        assert m["mae"] <= 2.0 and m["lf_ssim"] >= 0.98, m
+    finally:
+        nx.mlp_destroy(h)
