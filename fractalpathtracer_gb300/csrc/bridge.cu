@@ -339,8 +339,10 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     if (!check(cudaMemsetAsync(c.counter, 0, 64, c.stream), "counter reset", error, error_len)) return 1;
     bool want_profile = profile_out != nullptr || hydrated.sdf_profile != 0u;
     if (want_profile) {
-        if (!ensure_buffer((void **)&c.profile, &c.cap_profile, 8 * sizeof(unsigned long long), error, error_len)) return 1;
-        if (!check(cudaMemsetAsync(c.profile, 0, 8 * sizeof(unsigned long long), c.stream), "profile reset", error, error_len)) return 1;
+        if (!ensure_buffer((void **)&c.profile, &c.cap_profile, kProfileSlots * sizeof(unsigned long long), error, error_len)) return 1;
+        if (!check(cudaMemsetAsync(c.profile, 0, kProfileSlots * sizeof(unsigned long long), c.stream), "profile reset", error,
+                   error_len))
+            return 1;
     }
     cudaEventRecord(c.ev0, c.stream);
     if (hydrated.focus_distance <= 0.0f) {
@@ -456,7 +458,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
                error_len))
         return 1;
     if (want_profile && profile_out) {
-        unsigned long long v[8];
+        unsigned long long v[kProfileSlots];
         if (!check(cudaMemcpy(v, c.profile, sizeof(v), cudaMemcpyDeviceToHost), "profile readback", error, error_len)) return 1;
         profile_out->primary_steps = v[0]; profile_out->secondary_steps = v[1]; profile_out->shadow_steps = v[2];
         profile_out->normal_evals = v[3]; profile_out->bounces = v[4]; profile_out->pixels = v[5];
@@ -467,6 +469,23 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         profile_out->distance_evals_by_phase[1] = v[1];
         profile_out->distance_evals_by_phase[2] = v[2];
         profile_out->distance_evals_by_phase[3] = v[3];
+        profile_out->normal_field_evals = v[3];   // one (dual-number) field evaluation per normal
+        for (int k = 0; k < 3; ++k) profile_out->orbit_iterations_by_phase[k] = v[8 + k];
+        profile_out->march_orbit_iterations = v[8] + v[9] + v[10];
+        profile_out->formula_slot_iterations[0] = profile_out->march_orbit_iterations;   // one formula slot
+        profile_out->refinement_steps = v[11];
+        profile_out->refinement_distance_evals = v[11];
+        profile_out->max_ray_steps = v[12];
+        // Render time apportioned by counted work units (src/metal_bridge.mm:5712-5733).
+        const double units[5] = {double(v[0]), double(v[1]), double(v[2]), double(profile_out->normal_field_evals), double(v[4])};
+        const double total = units[0] + units[1] + units[2] + units[3] + units[4];
+        if (total > 0.0) {
+            profile_out->primary_ms_estimate = ms * units[0] / total;
+            profile_out->secondary_ms_estimate = ms * units[1] / total;
+            profile_out->shadow_ms_estimate = ms * units[2] / total;
+            profile_out->normal_ms_estimate = ms * units[3] / total;
+            profile_out->bounce_ms_estimate = ms * units[4] / total;
+        }
     }
     if (output_path) {
         if (unique_colour_sample(rgba, pixels) < 2) {

@@ -844,6 +844,16 @@ __device__ __forceinline__ Eval ext_eval(const DeviceScene &S, float3 p) {
     return e;
 }
 
+// Orbit iterations of an evaluation, for the profile counters
+// (shaders/Shaders.metal:7026), recovered from Eval::orbit (completed
+// iterations over the configured count); 0 for scenes without an orbit.
+__device__ __forceinline__ uint32_t orbit_iterations(const DeviceScene &S, const Eval &e) {
+    float n = 0.0f;
+    if (S.sdf_id == FPT_SDF_MANDELBULBER) n = fmaxf(S.set_values[1], 1.0f);
+    else if (S.formula != 0u) n = float(max(ext_iterations(S), 1));
+    return n > 0.0f ? uint32_t(__float2int_rn(e.orbit * n)) : 0u;
+}
+
 // scene_eval<KIND>(S, p, EV_MAP).d of an extension formula in two halves
 // around its orbit (ext_field, mandel_finish, ground plane, render[6]).
 template <int KIND> __device__ __forceinline__ int ext_eval_begin(const DeviceScene &S, float3 p, Orbit<float> &o) {
