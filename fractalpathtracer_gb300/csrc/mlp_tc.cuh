@@ -29,7 +29,7 @@ constexpr uint32_t kTcIdesc = umma::idesc_bf16_f32(kTcRows, kHid);
 constexpr unsigned long long kMmaWaitNs = 1000000000ull;   // 1 s; a layer takes about a microsecond
 
 struct TcSmem {
-    alignas(1024) unsigned char act[kTcRows * kInPad * 2];   // layer-0 features (K = 112), then hidden rows (K = 64)
+    alignas(128) unsigned char act[kTcRows * kInPad * 2];    // layer-0 features (K = 112), then hidden rows (K = 64)
     alignas(128) unsigned char w0[kHid * kInPad * 2];
     alignas(128) unsigned char w[kHidden - 1][kHid * kHid * 2];
     float b[kHidden][kHid];

@@ -354,7 +354,7 @@ __device__ __forceinline__ uint32_t feed_take(SkipFeed &F, bool need, const Wave
 // Guard word bits: 1 = loop time limit, 2 = an MMA did not complete.
 template <int KIND>
 __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WaveParams W, SkipArgs A) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
     const DeviceScene &S = *W.scene;
     const uint32_t total = W.counters[C_SKIPN];
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_primary_kernel(const 
 template <int KIND>
 __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_primary_tc_kernel(const DeviceScene *scene, SkipArgs A,
                                                                           FptCudaPrimaryHit *hits) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
     const DeviceScene &S = *scene;
     mlp::tc_setup(sm, A.M);
