@@ -38,6 +38,7 @@ struct Eval {
     float d;
     float orbit;
     int id;
+    int iters;   // orbit iterations of an extension-formula evaluation (profile counters), else 0
 };
 
 // ---------------------------------------------------------------- analytic scenes
@@ -505,6 +506,7 @@ __device__ __forceinline__ Eval mandel_finish(const DeviceScene &S, float3 p, Fi
         else if (e.d < th) e.d = th * 1.01f;
     }
     e.orbit = fabsf(f.state) / fmaxf(S.set_values[1], 1.0f);
+    e.iters = int(fabsf(f.state));
     return e;
 }
 
@@ -835,23 +837,13 @@ __device__ __forceinline__ Eval ext_eval(const DeviceScene &S, float3 p) {
             case KIND_MENGER: o = orbit_eval<KIND_MENGER, float>(S, p.x, p.y, p.z, ext_iterations(S), ext_bailout(S)); break;
             default: o = orbit_eval<KIND_HYBRID, float>(S, p.x, p.y, p.z, ext_iterations(S), ext_bailout(S)); break;
         }
-        e = {o.d, float(o.iterations) / float(max(ext_iterations(S), 1)), 0};
+        e = {o.d, float(o.iterations) / float(max(ext_iterations(S), 1)), 0, o.iterations};
     }
     if (S.ground_plane) {
         float plane = p.y - S.plane_height;
         if (plane < e.d) { e.d = plane; e.id = 1; }
     }
     return e;
-}
-
-// Orbit iterations of an evaluation, for the profile counters
-// (shaders/Shaders.metal:7026), recovered from Eval::orbit (completed
-// iterations over the configured count); 0 for scenes without an orbit.
-__device__ __forceinline__ uint32_t orbit_iterations(const DeviceScene &S, const Eval &e) {
-    float n = 0.0f;
-    if (S.sdf_id == FPT_SDF_MANDELBULBER) n = fmaxf(S.set_values[1], 1.0f);
-    else if (S.formula != 0u) n = float(max(ext_iterations(S), 1));
-    return n > 0.0f ? uint32_t(__float2int_rn(e.orbit * n)) : 0u;
 }
 
 // scene_eval<KIND>(S, p, EV_MAP).d of an extension formula in two halves

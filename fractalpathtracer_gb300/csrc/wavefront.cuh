@@ -335,7 +335,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
     bool have_d = false;
     bool active = false, pending = false, retired = false;
     uint32_t c_primary = 0, c_secondary = 0, c_shadow = 0, c_paths = 0;
-    uint32_t c_orbit[3] = {0u, 0u, 0u}, c_refine = 0, c_max_steps = 0;
+    // Profile counters kept off the registers of the march: orbit iterations of
+    // the lane's current job in one register, block totals in shared memory
+    // (updated when a march finishes, flushed at the end).
+    __shared__ unsigned int s_prof[5];   // orbit iterations primary / secondary / shadow, refinement steps, longest march
+    uint32_t c_job_orbit = 0;
+    if (threadIdx.x < 5) s_prof[threadIdx.x] = 0u;
+    __syncthreads();
     uint32_t trips = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
@@ -424,9 +430,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
         TranslucencyProbe<KIND> probe{sp};
         // One distance evaluation for every lane with a march in flight.
         if (active) {
-            const Eval ev = have_d ? Eval{known_d, 0.0f, 0} : scene_eval<KIND>(S, m.pos, EV_MAP);
+            const Eval ev = have_d ? Eval{known_d, 0.0f, 0, 0} : scene_eval<KIND>(S, m.pos, EV_MAP);
             const float d = ev.d;
-            if (W.profile && !have_d) c_orbit[job.shadow ? 2 : (job.bounce == 0u ? 0 : 1)] += orbit_iterations(S, ev);
+            c_job_orbit += uint32_t(ev.iters);
             have_d = false;
             active = march_update(m, S, d, probe);
             if (active && W.box_on && dot(m.pos - box_origin, m.dir) > box_exit) {
@@ -452,9 +458,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
         if (finish) {
             pending = false;
             if (W.profile) {
-                c_refine += uint32_t(m.refine);
-                c_max_steps = max(c_max_steps, uint32_t(m.steps));
+                atomicAdd(&s_prof[job.shadow ? 2 : (job.bounce == 0u ? 0 : 1)], c_job_orbit);
+                if (m.refine) atomicAdd(&s_prof[3], uint32_t(m.refine));
+                atomicMax(&s_prof[4], uint32_t(m.steps));
             }
+            c_job_orbit = 0;
             if (job.shadow) {
                 c_shadow += m.steps;
                 if (len3(job.rp0 - m.pos) > S.render[4] * 0.99f) {
@@ -486,17 +494,23 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
         }
     }
     if (W.profile) {
-        uint32_t v[8] = {c_primary, c_secondary, c_shadow, c_paths, c_orbit[0], c_orbit[1], c_orbit[2], c_refine};
-        const int slot[8] = {0, 1, 2, 5, 8, 9, 10, 11};
+        uint32_t v[4] = {c_primary, c_secondary, c_shadow, c_paths};
+        const int slot[4] = {0, 1, 2, 5};
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
+        for (int k = 0; k < 4; ++k) {
             uint32_t s = v[k];
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
             if (lane == 0 && s) atomicAdd(W.profile + slot[k], (unsigned long long)s);
         }
-        uint32_t mx = c_max_steps;
-        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, o));
-        if (lane == 0 && mx) atomicMax(W.profile + 12, (unsigned long long)mx);
+    }
+    __syncthreads();   // every lane of the block has left the loop
+    if (W.profile && threadIdx.x < 5) {
+        const unsigned long long s = s_prof[threadIdx.x];
+        if (threadIdx.x < 4) {
+            if (s) atomicAdd(W.profile + 8 + threadIdx.x, s);
+        } else if (s) {
+            atomicMax(W.profile + 12, s);
+        }
     }
 }
 

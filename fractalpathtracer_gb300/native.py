@@ -124,12 +124,18 @@ def metal_render(config: ffi.FptRenderConfig, output_path: str, linear_output: b
 
 
 def cuda_render(config: ffi.FptRenderConfig, ext: ffi.FptCudaSceneExt | None = None, output_path: str | None = None,
-                linear: bool = True, profile: bool = False):
-    """fpt_cuda_render: returns (linear HxWx4 float32 accumulation or None, rgba HxWx4 uint8 top row first, elapsed ms[, profile])."""
+                linear: bool = True, profile: bool = False, out_linear: np.ndarray | None = None,
+                out_rgba: np.ndarray | None = None):
+    """fpt_cuda_render: returns (linear HxWx4 float32 accumulation or None, rgba HxWx4 uint8 top row first, elapsed ms[, profile]).
+    out_linear / out_rgba: caller-owned contiguous arrays (W*H*4 float32 / uint8, e.g. pinned host memory) to
+    receive the results instead of new arrays."""
     L = lib()
     n = config.width * config.height * 4
-    lin = np.zeros(n, np.float32) if linear else None
-    rgba = np.zeros(n, np.uint8)
+    for a, dt in ((out_linear, np.float32), (out_rgba, np.uint8)):
+        if a is not None and (a.dtype != dt or a.size != n or not a.flags["C_CONTIGUOUS"]):
+            raise ValueError(f"output array must be a contiguous {np.dtype(dt).name} array of {n} elements")
+    lin = (out_linear.reshape(-1) if out_linear is not None else np.zeros(n, np.float32)) if linear else None
+    rgba = out_rgba.reshape(-1) if out_rgba is not None else np.zeros(n, np.uint8)
     elapsed = C.c_double()
     prof = ffi.FptSdfProfileStats()
     e = _err()
