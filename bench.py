@@ -376,7 +376,7 @@ def other_configs(native, nx, scenes, peaks):
     """Device-timed lines for the other workloads of the path (not the headline): 320x240 power-8 Mandelbulb
     primary rays; Menger fold + ground plane path tracing at 1280x720 16 spp; the 1024^3 Mandelbox occupancy-brick
     build and 1080p primary + shadow DDA (with its HBM roofline: 4 B brick-table read + 3 B occupancy / fp16
-    distance per visited cell, 32 B output per pixel)."""
+    distance per visited cell, 32 B output per pixel); 64 batched scenes; the learned skip on the Mandelbox."""
     med = lambda v: sorted(v)[len(v) // 2]
     out = {}
     cfg, ext = scenes.mandelbulb_primary(320, 240)
@@ -405,6 +405,18 @@ def other_configs(native, nx, scenes, peaks):
         "render_ms": ms, "Mrays_per_s": 2 * hits.size / ms / 1e3, "cells_visited": cells,
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                      "work": "7 B per visited cell + 32 B per pixel"}}
+    # 64 batched scenes (seeded types, powers, iterations, 64^2..512^2, 4 spp, 3 bounces) in one persistent pass
+    # per sample, each pass a CUDA graph; launch shape from the autotuner.
+    bundles = scenes.batch_scenes(64)
+    tune = nx.autotune_batch(bundles, rounds=2)
+    nx.render_batch(bundles, linear=False)
+    runs = [nx.render_batch(bundles, linear=False)[2] for _ in range(3)]
+    st = sorted(runs, key=lambda r: r["elapsed_ms"])[1]
+    out["batch_64_scenes_4spp"] = {"ms": st["elapsed_ms"], "Mpaths_per_s": st["paths"] / st["elapsed_ms"] / 1e3,
+                                   "paths": st["paths"], "graph_launches": st["graph_launches"],
+                                   "kernel_launches_per_pass": st["kernel_launches_per_pass"],
+                                   "tuned_block": st["block_size"], "tuned_registers": st["registers"],
+                                   "tuned_wave_paths": st["wave_paths"], "candidates": len(tune["tried"])}
     # The learned skip on the Mandelbox (scale -1.5, 12 iterations): the same recipe, its own model.
     b = scenes.mandelbox_path(W, H, SPP, BOUNCES)
     model, train = nx.mlp_create(b.cfg, b.ext, surrogate_config("mandelbox"))
