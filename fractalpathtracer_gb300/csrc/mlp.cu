@@ -334,6 +334,45 @@ __global__ void __launch_bounds__(kTcRows) predict_tc_kernel(Model M, const floa
     tc_teardown(sm);
     if (fail && threadIdx.x == 0) atomicOr(fail_word, 2u);
 }
+// Bounded-wait check (no fault): one CTA holds tensor memory and waits on an
+// mbarrier with a 20 ms limit, once after an arrival and once with none.
+// out[0] / out[1]: 1 = the phase completed, 2 = the wait ran out; out[2] /
+// out[3]: nanoseconds each wait took.  The tensor memory is freed either way.
+__global__ void __launch_bounds__(128) bounded_wait_kernel(uint32_t *out) {
+    __shared__ uint64_t bar[2];
+    __shared__ uint32_t tmem;
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar[0], 1u);
+        umma::mbar_init(&bar[1], 1u);
+    }
+    if (threadIdx.x < 32) {
+        __syncwarp();
+        umma::tmem_alloc(&tmem, 32u);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (threadIdx.x == 0) {
+        umma::mbar_arrive(&bar[0]);   // the first barrier's phase completes; nothing arrives on the second
+        for (int k = 0; k < 2; ++k) {
+            unsigned long long t0, t1;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+            const bool ok = umma::mbar_wait(&bar[k], 0u, 20000000ull);
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+            out[k] = ok ? 1u : 2u;
+            out[2 + k] = uint32_t(min(t1 - t0, 0xffffffffull));
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        __syncwarp();
+        umma::fence_after_sync();
+        umma::tmem_dealloc(tmem, 32u);
+    }
+}
+
 size_t forward_smem_bytes() { return ((sizeof(SmemWeights) + 127) & ~size_t(127)) + 4 * sizeof(WarpForward); }
 size_t train_smem_bytes() { return ((sizeof(SmemWeights) + 127) & ~size_t(127)) + kWarpsTrain * sizeof(WarpTrain); }
 
@@ -664,6 +703,23 @@ int fpt_cuda_mlp_predict(uint64_t model, const float *points_xyzw, size_t n, flo
         if (guard) { set_error(error, error_len, "a surrogate network MMA did not complete within 1 s"); return 1; }
     }
     return 0;
+}
+
+int fpt_test_bounded_waits(uint32_t *result, size_t result_len, char *error, size_t error_len) {
+    if (!result || result_len < 4) { set_error(error, error_len, "result needs 4 entries"); return 1; }
+    std::memset(result, 0, 4 * sizeof(uint32_t));
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    if (!ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len) ||
+        !check(cudaMemsetAsync(c.counter, 0, 4 * sizeof(uint32_t), c.stream), "result reset", error, error_len))
+        return 1;
+    mlp::bounded_wait_kernel<<<1, 128, 0, c.stream>>>(c.counter);
+    if (!check(cudaGetLastError(), "bounded-wait launch", error, error_len) ||
+        !check(cudaMemcpyAsync(result, c.counter, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream), "result readback", error,
+               error_len))
+        return 1;
+    return check(cudaStreamSynchronize(c.stream), "bounded-wait kernel", error, error_len) ? 0 : 1;
 }
 
 int fpt_cuda_mlp_get_params(uint64_t model, float *params, size_t len, char *error, size_t error_len) {

@@ -89,6 +89,7 @@ def declare(L: C.CDLL) -> None:
     L.fpt_cuda_set_launch_shape.argtypes = [C.c_uint32, C.c_int32]
     L.fpt_cuda_set_march_schedule.argtypes = [C.c_uint32, C.c_uint32]
     L.fpt_cuda_set_network_engine.argtypes = [C.c_uint32]
+    L.fpt_test_bounded_waits.argtypes = [P(C.c_uint32), C.c_size_t] + err
     L.fpt_cuda_render_batch.argtypes = [cfg, ext, C.c_size_t, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_size_t,
                                         P(FptCudaBatchStats)] + err
     L.fpt_cuda_autotune_batch.argtypes = [cfg, ext, C.c_size_t, C.c_uint32, P(FptCudaTuneResult)] + err
@@ -96,7 +97,7 @@ def declare(L: C.CDLL) -> None:
                  "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
                  "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
                  "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch", "fpt_cuda_set_launch_shape",
-                 "fpt_cuda_set_march_schedule", "fpt_cuda_set_network_engine"):
+                 "fpt_cuda_set_march_schedule", "fpt_cuda_set_network_engine", "fpt_test_bounded_waits"):
         getattr(L, name).restype = C.c_int
 
 
@@ -312,6 +313,15 @@ def set_launch_shape(wave_paths: int = 0, march_blocks: int = 0) -> None:
 
 NET_TCGEN05 = 0
 NET_MMA_SYNC = 1
+
+
+def bounded_wait_check() -> dict:
+    """fpt_test_bounded_waits: an mbarrier wait after an arrival and one with none (20 ms limit)."""
+    from .native import lib
+    r = (C.c_uint32 * 4)()
+    e = _err()
+    _check(lib().fpt_test_bounded_waits(r, 4, e, len(e)), e)
+    return {"arrived": r[0], "not_arrived": r[1], "arrived_ns": r[2], "not_arrived_ns": r[3]}
 
 
 def set_network_engine(engine: int = NET_TCGEN05) -> None:

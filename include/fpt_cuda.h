@@ -822,6 +822,12 @@ int fpt_cuda_mlp_gradients(uint64_t model,
                            char *error,
                            size_t error_len);
 int fpt_cuda_skip_stats(struct FptCudaSkipStats *stats);
+/* Test hook for the bounded waits of the tensor-core kernels (no fault is
+ * made): one CTA holding tensor memory waits 20 ms at most on an mbarrier,
+ * once after an arrival and once with none.  result[0] / result[1]: 1 = the
+ * wait completed, 2 = it ran out; result[2] / result[3]: ns each wait took.
+ * The kernel frees its tensor memory and the context stays usable. */
+int fpt_test_bounded_waits(uint32_t *result, size_t result_len, char *error, size_t error_len);
 
 /* Launch and timing record of the last fpt_cuda_render / fpt_metal_render
  * (no counterpart in the reference).  Kernel times are sums of CUDA-event

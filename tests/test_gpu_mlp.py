@@ -228,3 +228,15 @@ def test_mandelbox_skip(native):
         assert m["mae"] <= 2.0 and m["lf_ssim"] >= 0.98, m
     finally:
         nx.mlp_destroy(h)
+
+
+def test_bounded_mbarrier_wait(blank_model):
+    """The tensor-core kernels' mbarrier waits are bounded: a wait that nothing completes runs out after its
+    limit and reports it, the kernel frees its tensor memory, and tcgen05 kernels run normally afterwards."""
+    r = nx.bounded_wait_check()
+    print(r)
+    assert r["arrived"] == 1 and r["arrived_ns"] < 5_000_000
+    assert r["not_arrived"] == 2 and 20_000_000 <= r["not_arrived_ns"] < 1_000_000_000
+    nx.set_network_engine(nx.NET_TCGEN05)
+    y = nx.mlp_predict(blank_model, _points(256, 7))
+    assert np.isfinite(y).all()
