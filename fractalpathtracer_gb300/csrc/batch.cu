@@ -185,6 +185,7 @@ uint32_t launch_pass(const BatchPlan &P, const MarchVariant &V, uint32_t wave_pa
     W.q_march[1] = W.q_march[0] + cap;
     W.q_shade = W.q_march[1] + cap;
     W.q_skip = nullptr;
+    W.loop_limit_ns = kLoopLimitNs;
     W.skip_queue = 0u;
     int sms = 0, dev = 0, per_sm = 0, shade_per_sm = 0;
     cudaGetDevice(&dev);

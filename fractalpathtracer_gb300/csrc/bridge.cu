@@ -365,6 +365,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height; pl.bounces = S.bounces;
     pl.accum = c.accum; pl.counters = c.counter; pl.march_blocks = c.march_blocks;
     pl.march_schedule = c.march_schedule; pl.ilv_batch = c.ilv_batch; pl.refill_batch = c.refill_batch;
+    pl.loop_limit_ns = c.loop_limit_ns;
     pl.profile = want_profile ? c.profile : nullptr;
     {
         // Wave scratch: path records and queues for up to wave_paths paths.
@@ -419,7 +420,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
             return 1;
         if (guard) {
             set_error(error, error_len, (guard & 2u) ? "a surrogate network MMA did not complete within 1 s (render aborted)"
-                                                     : "a persistent march loop exceeded its 10 s limit and stopped (render aborted)");
+                                                     : "a persistent march loop exceeded its time limit and stopped (render aborted)");
             return 1;
         }
     }
@@ -841,6 +842,12 @@ int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch) {
     ctx().march_schedule = schedule;
     if (schedule == 1u) ctx().ilv_batch = batch;
     else ctx().refill_batch = batch;
+    return 0;
+}
+
+int fpt_cuda_set_loop_limit(uint64_t limit_ns) {
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    ctx().loop_limit_ns = limit_ns;
     return 0;
 }
 

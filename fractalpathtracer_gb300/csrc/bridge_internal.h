@@ -38,6 +38,7 @@ struct Context {
     uint32_t march_schedule = 0;   // 0: lockstep, 1: orbit-interleaved (extension formulas)
     uint32_t ilv_batch = 0;
     uint32_t refill_batch = 0;
+    unsigned long long loop_limit_ns = 0;   // persistent-loop time limit of later renders (0: 10 s)
     uint32_t network_engine = 0;   // FPT_CUDA_NET_*: surrogate network on tcgen05 (0) or mma.sync (1)
 };
 

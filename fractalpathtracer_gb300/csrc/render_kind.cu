@@ -35,6 +35,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     W.skip_queue = skip_pass ? 1u : 0u;
     W.ilv_batch = pl.ilv_batch;
     W.refill_batch = pl.refill_batch;
+    W.loop_limit_ns = pl.loop_limit_ns ? pl.loop_limit_ns : kLoopLimitNs;
     // extension formulas can march with the orbit-interleaved kernel (schedule 1)
     constexpr bool kExt = KIND == KIND_BULB8 || KIND == KIND_BULB || KIND == KIND_BOX || KIND == KIND_MENGER || KIND == KIND_HYBRID;
     const bool interleaved = kExt && pl.march_schedule == 1u;

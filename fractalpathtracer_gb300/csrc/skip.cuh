@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WavePara
     uint32_t trips = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
-        if (loop_guard(trips, t0, W.counters)) break;
+        if (loop_guard(trips, t0, W.counters, W.loop_limit_ns)) break;
         skip_refill(L, A, W, total, lane, retired, job, c_esc);
         if (!__any_sync(FULL, L.phase != SP_IDLE)) {
             if (__all_sync(FULL, retired)) break;
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WavePara
     const unsigned long long t0 = global_ns();
     while (true) {
         if ((++trips & 1023u) == 0u) {   // the same trip in every thread
-            if (__syncthreads_or(global_ns() - t0 > kLoopLimitNs)) {
+            if (__syncthreads_or(global_ns() - t0 > W.loop_limit_ns)) {
                 if (threadIdx.x == 0) atomicOr(W.counters + C_GUARD, 1u);
                 break;
             }

@@ -86,9 +86,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 // Every 1024 trips: true (for the whole warp) once the loop has run past the
 // limit; the first lane to see it records the error.
-__device__ __forceinline__ bool loop_guard(uint32_t &trips, unsigned long long t0, uint32_t *counters) {
+__device__ __forceinline__ bool loop_guard(uint32_t &trips, unsigned long long t0, uint32_t *counters, unsigned long long limit_ns) {
     if ((++trips & 1023u) != 0u) return false;
-    const bool over = global_ns() - t0 > kLoopLimitNs;
+    const bool over = global_ns() - t0 > limit_ns;
     if (!__any_sync(0xffffffffu, over)) return false;
     if ((threadIdx.x & 31u) == 0u) atomicOr(counters + C_GUARD, 1u);
     return true;
@@ -125,6 +125,7 @@ struct WaveParams {
     const uint32_t *pass;        // sample index of the pass (device word, advanced by the pass graph)
     uint32_t ilv_batch;          // orbit-interleaved march: lanes that finish together (0: 16)
     uint32_t refill_batch;       // lockstep march: finished lanes wait for this many (0: kRefillBatch, 1: none)
+    unsigned long long loop_limit_ns;   // time limit of the persistent loops (guard word bit 1 when reached)
 };
 
 // Scene of work index g: the largest k with base[k] <= g (base[0] = 0).
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
     uint32_t trips = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
-        if (loop_guard(trips, t0, W.counters)) break;
+        if (loop_guard(trips, t0, W.counters, W.loop_limit_ns)) break;
         // Refill every lane whose march finished: one atomic per warp.
         unsigned need = __ballot_sync(FULL, !active && !pending && !retired);
         if (need) {
@@ -553,7 +554,7 @@ __global__ void __launch_bounds__(128, 7) march_ilv_kernel(WaveParams W, int cur
     uint32_t trips = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
-        if (loop_guard(trips, t0, W.counters)) break;
+        if (loop_guard(trips, t0, W.counters, W.loop_limit_ns)) break;
         unsigned need = __ballot_sync(FULL, !active && !pending && !retired);
         if (need) {
             uint32_t leader = __ffs(need) - 1, base = 0;

@@ -28,6 +28,7 @@ EXPORTED = [
     "fpt_cuda_set_march_schedule",
     "fpt_cuda_set_network_engine",
     "fpt_test_bounded_waits",
+    "fpt_cuda_set_loop_limit",
 ]
 
 

@@ -90,6 +90,7 @@ def declare(L: C.CDLL) -> None:
     L.fpt_cuda_set_march_schedule.argtypes = [C.c_uint32, C.c_uint32]
     L.fpt_cuda_set_network_engine.argtypes = [C.c_uint32]
     L.fpt_test_bounded_waits.argtypes = [P(C.c_uint32), C.c_size_t] + err
+    L.fpt_cuda_set_loop_limit.argtypes = [C.c_uint64]
     L.fpt_cuda_render_batch.argtypes = [cfg, ext, C.c_size_t, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_size_t,
                                         P(FptCudaBatchStats)] + err
     L.fpt_cuda_autotune_batch.argtypes = [cfg, ext, C.c_size_t, C.c_uint32, P(FptCudaTuneResult)] + err
@@ -97,7 +98,8 @@ def declare(L: C.CDLL) -> None:
                  "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
                  "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
                  "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch", "fpt_cuda_set_launch_shape",
-                 "fpt_cuda_set_march_schedule", "fpt_cuda_set_network_engine", "fpt_test_bounded_waits"):
+                 "fpt_cuda_set_march_schedule", "fpt_cuda_set_network_engine", "fpt_test_bounded_waits",
+                 "fpt_cuda_set_loop_limit"):
         getattr(L, name).restype = C.c_int
 
 
@@ -313,6 +315,12 @@ def set_launch_shape(wave_paths: int = 0, march_blocks: int = 0) -> None:
 
 NET_TCGEN05 = 0
 NET_MMA_SYNC = 1
+
+
+def set_loop_limit(limit_ns: int = 0) -> None:
+    """Time limit of the persistent loops of later renders in ns (0: 10 s)."""
+    from .native import lib
+    lib().fpt_cuda_set_loop_limit(limit_ns)
 
 
 def bounded_wait_check() -> dict:

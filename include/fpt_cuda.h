@@ -874,6 +874,11 @@ int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch);
 #define FPT_CUDA_NET_MMA_SYNC 1u
 int fpt_cuda_set_network_engine(uint32_t engine);
 
+/* Time limit of the persistent loops of later single-scene renders, in ns
+ * (0: 10 s).  A loop that reaches it stops, and the render returns 1 with
+ * "exceeded its time limit"; the context stays usable. */
+int fpt_cuda_set_loop_limit(uint64_t limit_ns);
+
 /* ---- Batched scenes (no counterpart in the reference; its render-batch
  * command only reuses the process, src/main.rs:2269) ----
  * count scenes (extension formulas, the same sample count, no sky image, no

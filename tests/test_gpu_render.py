@@ -158,3 +158,19 @@ def test_profile_stats(native):
     est = p["primary_ms_estimate"] + p["secondary_ms_estimate"] + p["shadow_ms_estimate"] + p["normal_ms_estimate"] + \
         p["bounce_ms_estimate"]
     assert abs(est - ms) <= 1e-6 * ms + 1e-9
+
+
+def test_loop_time_limit(native):
+    """A persistent loop that reaches its time limit stops and the render reports it (no fault); with the default
+    limit back, the next render is the same as before."""
+    from fractalpathtracer_gb300 import native_ext as nx
+    b = scenes.mandelbulb_path(960, 540, 16, 4)   # enough rays per lane for the 1024-trip check interval
+    _, before, _ = native.cuda_render(b.cfg, b.ext, linear=False)
+    nx.set_loop_limit(2000)   # 2 us: the loops stop at their first check after 1024 trips
+    try:
+        with pytest.raises(native.NativeError, match="time limit"):
+            native.cuda_render(b.cfg, b.ext, linear=False)
+    finally:
+        nx.set_loop_limit(0)
+    _, after, _ = native.cuda_render(b.cfg, b.ext, linear=False)
+    assert np.array_equal(before, after)
