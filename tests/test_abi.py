@@ -97,3 +97,19 @@ def test_flat_union_lowering_matches_program():
         d_soa = np.minimum(d_soa, (pts - c) @ n + t.plane_offset[i])
     assert t.sphere_count + t.box_count + t.plane_count == 12
     assert np.abs(d_prog - d_soa).max() < 1e-5
+
+
+def test_settings_validate_arguments_without_gpu(native):
+    """Host-side settings reject out-of-range values before any CUDA call (runs without a GPU)."""
+    import pytest
+    from fractalpathtracer_gb300 import native_ext as nx
+    with pytest.raises(ValueError):
+        nx.set_network_engine(7)
+    with pytest.raises(ValueError):
+        nx.set_march_schedule(3, 0)
+    with pytest.raises(ValueError):
+        nx.set_march_schedule(0, 33)
+    nx.set_network_engine(nx.NET_MMA_SYNC)
+    nx.set_network_engine(nx.NET_TCGEN05)
+    nx.set_march_schedule(0, 0)
+    nx.set_loop_limit(0)
