@@ -72,3 +72,20 @@ def test_analytic_gradient_matches_fp64(native):
     ok = (nr > 1e-6) & np.isfinite(ng)
     cosang = (gg[ok] * gr[ok]).sum(1) / (ng[ok] * nr[ok])
     assert np.percentile(np.degrees(np.arccos(np.clip(cosang, -1, 1))), 99) < 0.5
+
+
+# Mandelbulbs of power 2.29, 10.6, 2.89, 5.24, 7.93; Mandelboxes; hybrids of 5, 12 and 16 iterations.
+@pytest.mark.parametrize("k", [11, 14, 21, 27, 30, 1, 9, 12, 0, 3, 4])
+def test_batch_scene_fields(native, k):
+    """The formulas of the batched workload against the FP64 oracle: Mandelbulbs of non-integer power (the
+    trigonometric step of orbit.rs:766-778), Mandelboxes of other scales, the bulb / Menger hybrid, with
+    4-16 iterations (scene k of scenes.batch_scene)."""
+    b = scenes.batch_scene(k)
+    p = pts(1 << 15, -1.6 if b.ext.formula != ffi.FORMULA_MANDELBOX else -4.0,
+            1.6 if b.ext.formula != ffi.FORMULA_MANDELBOX else 4.0, seed=20 + k)
+    g = native.sample_distance(b.cfg, b.ext, p)
+    r = oracle.sample_distance(b.cfg, b.ext, p, fp64=True)
+    print(k, b.ext.formula, b.ext.power, b.ext.iterations,
+          np.percentile(np.abs(g[:, 0] - r[:, 0]) / (1 + np.abs(r[:, 0])), 99))
+    _gate(g[:, 0], r[:, 0], outliers=5e-3)
+    assert np.mean(g[:, 3] == r[:, 3]) > 0.99   # iteration counts
