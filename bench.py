@@ -110,6 +110,9 @@ def measured_peaks():
         return {}
 
 
+WORKLOAD = f"power-8 Mandelbulb path tracing {W}x{H} {SPP}spp {BOUNCES} bounces, RR after 2"
+
+
 def run_reference(args, world, rank):
     """CPU arm: the oracle's FP32 restatement of the path, all host threads, bounded sample of the workload."""
     if rank != 0:
@@ -134,7 +137,8 @@ def run_reference(args, world, rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total / len(times) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"power-8 Mandelbulb path tracing {W}x{H} {SPP}spp {BOUNCES} bounces", "march": "plain"},
+        "config": {"workload": WORKLOAD, "march": "plain (the reference has no surrogate)",
+                   "parallelism": f"{cores} host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"rows {rows[0]}-{rows[1]} of {H}, every {stride}th column, all {SPP} samples"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -303,7 +307,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": s_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"power-8 Mandelbulb path tracing {W}x{H} {SPP}spp {BOUNCES} bounces, RR after 2",
+        "config": {"workload": WORKLOAD,
                    "march": "surrogate-skip (value) vs plain", "l2": "flushed (256 MB write) between steps",
                    "parallelism": f"replicas x{world}",
                    "surrogate": "3->99 Fourier->4x64 SiLU->1 bf16, 16M points (50% near-surface), 4000 Adam steps"},
