@@ -420,7 +420,9 @@ def other_configs(native, nx, scenes, peaks):
                                    "paths": st["paths"], "graph_launches": st["graph_launches"],
                                    "kernel_launches_per_pass": st["kernel_launches_per_pass"],
                                    "tuned_block": st["block_size"], "tuned_registers": st["registers"],
-                                   "tuned_wave_paths": st["wave_paths"], "candidates": len(tune["tried"])}
+                                   "tuned_wave_paths": st["wave_paths"], "candidates": len(tune["tried"]),
+                                   "candidate_median_ms": [round(c["median_ms"], 2) for c in tune["tried"]],
+                                   "chosen": tune["chosen"]}
     # The learned skip on the Mandelbox (scale -1.5, 12 iterations): the same recipe, its own model.
     b = scenes.mandelbox_path(W, H, SPP, BOUNCES)
     model, train = nx.mlp_create(b.cfg, b.ext, surrogate_config("mandelbox"))
