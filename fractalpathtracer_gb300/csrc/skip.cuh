@@ -6,15 +6,17 @@
 //   s <= d_p + DE(q)   the balls of radius d_p around p and DE(q) around q
 //                      hold no surface and overlap, so [p, q] is free:
 //                      the ray moves to q (one exact evaluation for s)
-//   otherwise          plain step 0.99 d_p (the reference march rule)
+//   otherwise          one step of the scene's march rule (march_update's
+//                      step, applied to the position the way it applies it)
 // lambda adapts per ray: 1.5 s / d_p after an accepted step (rays leaving a
-// surface look further ahead each step), 2 after a refusal.  The exact march
-// takes over where the distance is under the hand-over margin.
+// surface look further ahead each step), 2 after a refusal.
 // Every step is certified by the exact DE, so the surrogate only changes how
-// far a ray gets per evaluation, never what it hits.  When d_p falls below
-// the hand-over margin the exact march (march_update) finishes the ray.
-// Geometry lies inside the model's box: a ray that misses or leaves it is a
-// miss without further evaluation.
+// far a ray gets per evaluation, never what it hits (where the DE is a lower
+// bound of the distance; steps it does not replace visit the plain march's
+// positions).  When d_p falls below the hand-over margin the exact march
+// resumes the ray with its step count and last step.  Camera rays start at
+// the plain march's first step; geometry lies inside the model's box, and a
+// camera ray that misses or leaves it is a miss without further evaluation.
 //
 // Two network engines: tcgen05 (default; 128 rows per CTA, accumulators in
 // tensor memory, a CTA-synchronous loop) and mma.sync (32 rows per warp, a
