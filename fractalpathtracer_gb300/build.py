@@ -36,8 +36,9 @@ def _units():
     # values that seed hashes use explicitly rounded intrinsics.
     fast = ["-prec-div=false", "-prec-sqrt=false"]
     units = []
-    for k in range(KINDS):
-        units.append(("render_kind.cu", f"render_kind{k}.o", fast + [f"-DFPT_KIND={k}"]))
+    for k in range(KINDS):   # each kind in three parts (path tracer, primary/samples/diagnostics, surrogate)
+        for part in range(3):
+            units.append(("render_kind.cu", f"render_kind{k}_{part}.o", fast + [f"-DFPT_KIND={k}", f"-DFPT_PART={part}"]))
     units.append(("render_common.cu", "render_common.o", fast))
     # Voxel build and DDA: IEEE operations in source order (no contraction),
     # so brick tables and cell sequences are bit-identical to the CPU path.

@@ -9,10 +9,24 @@
 #ifndef FPT_KIND
 #error "FPT_KIND must be defined"
 #endif
+// FPT_PART splits a kind's kernels over three objects that build in parallel:
+// 0 the path tracer, 1 primary rays / samples / diagnostics, 2 the surrogate
+// kernels (skip passes, labels).
+#ifndef FPT_PART
+#error "FPT_PART must be defined"
+#endif
+
+#define FPT_CAT2(a, b) a##b
+#define FPT_CAT(a, b) FPT_CAT2(a, b)
 
 namespace fpt {
 
-cudaError_t launch_pathtrace_kind(const PathLaunch &pl, cudaStream_t stream, int kind_tag);
+// The skip pass of the path tracer (part 2): persistent blocks for the engine,
+// and the launch.
+int FPT_CAT(skip_pass_blocks_k, FPT_KIND)(bool tc, int sms);
+void FPT_CAT(launch_skip_pass_k, FPT_KIND)(const WaveParams &W, const SkipArgs &A, bool tc, int blocks, cudaStream_t stream);
+
+#if FPT_PART == 0
 
 template <int KIND>
 static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
@@ -57,22 +71,8 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<KIND>, 128, 0);
         march_blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
-    int skip_blocks = 0;
     const bool skip_tc = skip_pass && pl.skip->engine == kNetTcgen05;
-    if (skip_pass) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(skip_march_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(skip_smem_bytes()));
-            cudaFuncSetAttribute(skip_march_tc_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mlp::tc_smem_bytes()));
-            attr = true;
-        }
-        int skip_per_sm = 0;
-        if (skip_tc)
-            skip_per_sm = mlp::tc_blocks_per_sm(reinterpret_cast<const void *>(skip_march_tc_kernel<KIND>));
-        else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&skip_per_sm, skip_march_kernel<KIND>, 32 * kSkipWarps, skip_smem_bytes());
-        skip_blocks = sms * (skip_per_sm > 0 ? skip_per_sm : 1);
-    }
+    const int skip_blocks = skip_pass ? FPT_CAT(skip_pass_blocks_k, FPT_KIND)(skip_tc, sms) : 0;
     if (pl.grids) {
         pl.grids[0] = uint32_t(march_blocks);
         pl.grids[1] = uint32_t(skip_blocks);
@@ -107,12 +107,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
             // margin), so the skip pass would hand them straight back: it runs on
             // the camera rays only, the box clip applies in every pass.
             if (skip_pass && b == 0u)
-                timed(KC_SKIP, [&] {
-                    if (skip_tc)
-                        skip_march_tc_kernel<KIND><<<skip_blocks, mlp::kTcRows, mlp::tc_smem_bytes(), stream>>>(W, *pl.skip);
-                    else
-                        skip_march_kernel<KIND><<<skip_blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, *pl.skip);
-                });
+                timed(KC_SKIP, [&] { FPT_CAT(launch_skip_pass_k, FPT_KIND)(W, *pl.skip, skip_tc, skip_blocks, stream); });
             timed(KC_MARCH, [&] {
                 if (interleaved) march_ilv_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
                 else march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
@@ -131,20 +126,20 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-#define FPT_CAT2(a, b) a##b
-#define FPT_CAT(a, b) FPT_CAT2(a, b)
-
 cudaError_t FPT_CAT(launch_pathtrace_k, FPT_KIND)(const PathLaunch &pl, cudaStream_t stream) {
     return launch_path_impl<FPT_KIND>(pl, stream);
 }
+cudaError_t FPT_CAT(launch_focus_k, FPT_KIND)(DeviceScene *scene, cudaStream_t st) {
+    focus_kernel<FPT_KIND><<<1, 32, 0, st>>>(scene);
+    return cudaGetLastError();
+}
+#endif  // FPT_PART == 0
+
+#if FPT_PART == 1
 cudaError_t FPT_CAT(launch_trace_primary_k, FPT_KIND)(const DeviceScene *scene, uint32_t W, uint32_t H, FptCudaPrimaryHit *hits,
                                                       cudaStream_t st) {
     dim3 grid((W + 15u) / 16u, (H + 7u) / 8u);
     trace_primary_kernel<FPT_KIND><<<grid, 128, 0, st>>>(scene, hits);
-    return cudaGetLastError();
-}
-cudaError_t FPT_CAT(launch_focus_k, FPT_KIND)(DeviceScene *scene, cudaStream_t st) {
-    focus_kernel<FPT_KIND><<<1, 32, 0, st>>>(scene);
     return cudaGetLastError();
 }
 cudaError_t FPT_CAT(launch_sample_distance_k, FPT_KIND)(const DeviceScene *scene, const float4 *pts, float4 *out, float *grads,
@@ -158,6 +153,36 @@ cudaError_t FPT_CAT(launch_diagnostic_k, FPT_KIND)(const DeviceScene *scene, uin
     dim3 grid((W + 15u) / 16u, (H + 7u) / 8u);
     diagnostic_kernel<FPT_KIND><<<grid, 128, 0, st>>>(scene, mode, max_distance, 0u, 0u, out);
     return cudaGetLastError();
+}
+#if FPT_KIND == 0
+cudaError_t launch_field_sample(const DeviceScene *scene, const float4 *pts, float4 *out, size_t n, cudaStream_t st) {
+    unsigned blocks = unsigned((n + 255) / 256);
+    field_sample_kernel<KIND_GENERIC><<<blocks, 256, 0, st>>>(scene, pts, out, n);
+    return cudaGetLastError();
+}
+#endif
+#endif  // FPT_PART == 1
+
+#if FPT_PART == 2
+int FPT_CAT(skip_pass_blocks_k, FPT_KIND)(bool tc, int sms) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(skip_march_kernel<FPT_KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(skip_smem_bytes()));
+        cudaFuncSetAttribute(skip_march_tc_kernel<FPT_KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mlp::tc_smem_bytes()));
+        attr = true;
+    }
+    int per_sm = 0;
+    if (tc)
+        per_sm = mlp::tc_blocks_per_sm(reinterpret_cast<const void *>(skip_march_tc_kernel<FPT_KIND>));
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, skip_march_kernel<FPT_KIND>, 32 * kSkipWarps, skip_smem_bytes());
+    return sms * (per_sm > 0 ? per_sm : 1);
+}
+void FPT_CAT(launch_skip_pass_k, FPT_KIND)(const WaveParams &W, const SkipArgs &A, bool tc, int blocks, cudaStream_t stream) {
+    if (tc)
+        skip_march_tc_kernel<FPT_KIND><<<blocks, mlp::kTcRows, mlp::tc_smem_bytes(), stream>>>(W, A);
+    else
+        skip_march_kernel<FPT_KIND><<<blocks, 32 * kSkipWarps, skip_smem_bytes(), stream>>>(W, A);
 }
 cudaError_t FPT_CAT(launch_label_k, FPT_KIND)(const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t st) {
     label_kernel<FPT_KIND><<<unsigned((n + 255) / 256), 256, 0, st>>>(scene, pts, n);
@@ -182,12 +207,6 @@ cudaError_t FPT_CAT(launch_skip_primary_k, FPT_KIND)(const DeviceScene *scene, u
     skip_primary_kernel<FPT_KIND><<<blocks, 32 * kSkipWarps, skip_smem_bytes(), st>>>(scene, args, hits);
     return cudaGetLastError();
 }
-#if FPT_KIND == 0
-cudaError_t launch_field_sample(const DeviceScene *scene, const float4 *pts, float4 *out, size_t n, cudaStream_t st) {
-    unsigned blocks = unsigned((n + 255) / 256);
-    field_sample_kernel<KIND_GENERIC><<<blocks, 256, 0, st>>>(scene, pts, out, n);
-    return cudaGetLastError();
-}
-#endif
+#endif  // FPT_PART == 2
 
 }  // namespace fpt
