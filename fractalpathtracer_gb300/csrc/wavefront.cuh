@@ -340,9 +340,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
     // the lane's current job in one register, block totals in shared memory
     // (updated when a march finishes, flushed at the end).
     __shared__ unsigned int s_prof[5];   // orbit iterations primary / secondary / shadow, refinement steps, longest march
+    __shared__ unsigned int s_warps_done;
     uint32_t c_job_orbit = 0;
-    if (threadIdx.x < 5) s_prof[threadIdx.x] = 0u;
-    __syncthreads();
+    if (W.profile) {   // the same in every thread
+        if (threadIdx.x < 5) s_prof[threadIdx.x] = 0u;
+        if (threadIdx.x == 0) s_warps_done = 0u;
+        __syncthreads();
+    }
     uint32_t trips = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
@@ -504,13 +508,23 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
             if (lane == 0 && s) atomicAdd(W.profile + slot[k], (unsigned long long)s);
         }
     }
-    __syncthreads();   // every lane of the block has left the loop
-    if (W.profile && threadIdx.x < 5) {
-        const unsigned long long s = s_prof[threadIdx.x];
-        if (threadIdx.x < 4) {
-            if (s) atomicAdd(W.profile + 8 + threadIdx.x, s);
-        } else if (s) {
-            atomicMax(W.profile + 12, s);
+    if (W.profile) {
+        // The block's last warp to leave the loop flushes the shared totals (no
+        // block barrier: finished warps do not wait for the others).
+        __threadfence_block();
+        uint32_t last = 0;
+        if (lane == 0) last = atomicAdd(&s_warps_done, 1u) == blockDim.x / 32u - 1u ? 1u : 0u;
+        last = __shfl_sync(FULL, last, 0);
+        if (last) {
+            __threadfence_block();
+            if (lane < 5) {
+                const unsigned long long s = atomicAdd(&s_prof[lane], 0u);   // read after the other warps' updates
+                if (lane < 4) {
+                    if (s) atomicAdd(W.profile + 8 + lane, s);
+                } else if (s) {
+                    atomicMax(W.profile + 12, s);
+                }
+            }
         }
     }
 }
