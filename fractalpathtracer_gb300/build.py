@@ -46,10 +46,11 @@ def _units():
     units.append(("mlp.cu", "mlp.o", []))
     units.append(("batch.cu", "batch.o", fast))
     units.append(("bridge.cu", "bridge.o", []))
-    units.append(("diagnostics.cu", "diagnostics.o", []))
     units.append(("image_io.cpp", "image_io.o", []))
-    units.append(("zz_pending.cu", "zz_pending.o", []))
-    return [u for u in units if os.path.exists(os.path.join(CSRC, u[0]))]
+    missing = sorted({u[0] for u in units if not os.path.exists(os.path.join(CSRC, u[0]))})
+    if missing:
+        raise RuntimeError(f"listed sources are missing from {CSRC}: {', '.join(missing)}")
+    return units
 
 
 def _compile(nvcc: str, unit, verbose: bool):

@@ -13,7 +13,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <new>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -24,6 +26,15 @@
 #include "bridge_internal.h"
 #include "skip.cuh"
 #include "diag.cuh"
+
+// Layout pins of the reference ABI (src/ffi.rs:494-507, static_asserts of
+// src/metal_bridge.mm:32-39): a caller compiled against the reference header
+// passes these structs by pointer.
+static_assert(sizeof(FptSdfInstruction) == 32, "FptSdfInstruction must be 32 bytes");
+static_assert(sizeof(FptRenderConfig) == 30448, "FptRenderConfig must be 30448 bytes");
+static_assert(sizeof(FptSdfProfileStats) == 288, "FptSdfProfileStats must be 288 bytes");
+static_assert(sizeof(FptDiagnosticConfig) == 24, "FptDiagnosticConfig must be 24 bytes");
+static_assert(sizeof(FptMandelbulberFieldSample) == 16, "FptMandelbulberFieldSample must be 16 bytes");
 
 namespace fpt {
 
@@ -42,9 +53,26 @@ Context &ctx() {
     return c;
 }
 
+// Device ordinal of the process-wide context: FPT_CUDA_DEVICE when set, else
+// LOCAL_RANK (one replica per GPU under torchrun), else 0, unless
+// fpt_cuda_set_device chose one before the context was created.  The library
+// links its own CUDA runtime, so the caller's runtime (torch's included) does
+// not select its device: every entry point binds it on the calling thread.
+static int default_device_ordinal(int count) {
+    for (const char *name : {"FPT_CUDA_DEVICE", "LOCAL_RANK"}) {
+        const char *v = std::getenv(name);
+        if (v && *v) {
+            char *end = nullptr;
+            long k = std::strtol(v, &end, 10);
+            if (end && *end == 0 && k >= 0) return int(k % count);
+        }
+    }
+    return 0;
+}
+
 bool ensure_device(char *error, size_t error_len) {
     Context &c = ctx();
-    if (c.ready) return true;
+    if (c.ready) return check(cudaSetDevice(c.device), "cudaSetDevice", error, error_len);
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess || count == 0) {
@@ -52,11 +80,37 @@ bool ensure_device(char *error, size_t error_len) {
                   e != cudaSuccess ? cudaGetErrorString(e) : "no device");
         return false;
     }
+    if (c.device < 0) c.device = default_device_ordinal(count);
+    if (c.device >= count) {
+        set_error(error, error_len, "CUDA device %d requested but only %d visible", c.device, count);
+        return false;
+    }
+    if (!check(cudaSetDevice(c.device), "cudaSetDevice", error, error_len)) return false;
     e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { set_error(error, error_len, "failed to create CUDA stream: %s", cudaGetErrorString(e)); return false; }
     cudaEventCreate(&c.ev0);
     cudaEventCreate(&c.ev1);
     c.ready = true;
+    return true;
+}
+
+// A shader source generated from a Mandelbulber formula: the reference compiles
+// it into the renderer (src/metal_bridge.mm:4231-4240, 5889-5897; the generator
+// defines FPT_MANDEL_GENERATED_FIELD, src/mandelbulber/compiler.rs:1510).  The
+// stock shader source (what src/main.rs passes on every other call) is what
+// these kernels restate.
+static bool generated_formula_source(const char *source, size_t len) {
+    if (!source || len == 0) return false;
+    static const char marker[] = "#define FPT_MANDEL_GENERATED_FIELD";
+    const size_t m = sizeof(marker) - 1;
+    if (len < m) return false;
+    return std::search(source, source + len, marker, marker + m) != source + len;
+}
+static bool reject_generated_source(const char *source, size_t len, char *error, size_t error_len) {
+    if (!generated_formula_source(source, len)) return false;
+    set_error(error, error_len,
+              "generated Mandelbulber formulas are not supported by the CUDA path (shader_source defines "
+              "FPT_MANDEL_GENERATED_FIELD); use the FptCudaSceneExt formulas with fpt_cuda_render");
     return true;
 }
 
@@ -246,7 +300,12 @@ bool hydrate_hdri(FptRenderConfig &config, char *error, size_t error_len) {
     if (!path[0]) { set_error(error, error_len, "HDRI world mode requires world.hdri"); return false; }
     HdrImage img;
     std::string err;
-    if (!read_radiance_hdr(path, img, err)) { set_error(error, error_len, "%s", err.c_str()); return false; }
+    try {
+        if (!read_radiance_hdr(path, img, err)) { set_error(error, error_len, "%s", err.c_str()); return false; }
+    } catch (const std::exception &ex) {
+        set_error(error, error_len, "failed to read HDRI %s: %s", path, ex.what());
+        return false;
+    }
     config.hdri_width = FPT_HDRI_LUT_WIDTH;
     config.hdri_height = FPT_HDRI_LUT_HEIGHT;
     for (uint32_t y = 0; y < FPT_HDRI_LUT_HEIGHT; ++y) {
@@ -364,7 +423,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     PathLaunch pl{};
     pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height; pl.bounces = S.bounces;
     pl.accum = c.accum; pl.counters = c.counter; pl.march_blocks = c.march_blocks;
-    pl.march_schedule = c.march_schedule; pl.ilv_batch = c.ilv_batch; pl.refill_batch = c.refill_batch;
+    pl.refill_batch = c.refill_batch;
     pl.loop_limit_ns = c.loop_limit_ns;
     pl.profile = want_profile ? c.profile : nullptr;
     {
@@ -514,7 +573,7 @@ int fpt_metal_render(const char *metallib_path, const char *stitch_metallib_path
                      struct FptStitchValidationStats *stitch_validation_stats, struct FptStitchPipelineStats *stitch_pipeline_stats,
                      struct FptSdfProfileStats *sdf_profile_stats, float *linear_output, size_t linear_output_len, char *error,
                      size_t error_len) {
-    (void)metallib_path; (void)stitch_metallib_path; (void)stitch_archive_path; (void)shader_source; (void)shader_source_len;
+    (void)metallib_path; (void)stitch_metallib_path; (void)stitch_archive_path;
     if (build_ms) *build_ms = 0.0;
     if (voxel_memory_bytes) *voxel_memory_bytes = 0;
     if (voxel_active_bricks) *voxel_active_bricks = 0;
@@ -524,6 +583,9 @@ int fpt_metal_render(const char *metallib_path, const char *stitch_metallib_path
     if (stitch_cache_status) *stitch_cache_status = 0;
     if (stitch_validation_stats) std::memset(stitch_validation_stats, 0, sizeof(*stitch_validation_stats));
     if (stitch_pipeline_stats) std::memset(stitch_pipeline_stats, 0, sizeof(*stitch_pipeline_stats));
+    if (elapsed_ms) *elapsed_ms = 0.0;
+    if (sdf_profile_stats) std::memset(sdf_profile_stats, 0, sizeof(*sdf_profile_stats));
+    if (reject_generated_source(shader_source, shader_source_len, error, error_len)) return 1;
     if (!output_path) { set_error(error, error_len, "missing output path"); return 1; }
     std::lock_guard<std::mutex> lock(ctx().mutex);
     return render_core(config, nullptr, output_path, linear_output, linear_output_len, nullptr, 0, elapsed_ms, sdf_profile_stats,
@@ -601,11 +663,12 @@ int fpt_cuda_trace_primary(const struct FptRenderConfig *config, const struct Fp
 int fpt_mandelbulber_sample_field(const char *metallib_path, const char *shader_source, size_t shader_source_len,
                                   const struct FptRenderConfig *config, const float *points_xyzw, size_t point_count,
                                   struct FptMandelbulberFieldSample *samples, char *error, size_t error_len) {
-    (void)metallib_path; (void)shader_source; (void)shader_source_len;
+    (void)metallib_path;
     if (!config || !points_xyzw || !samples || point_count == 0u) {
         set_error(error, error_len, "missing Mandelbulber field-sampling input");
         return 1;
     }
+    if (reject_generated_source(shader_source, shader_source_len, error, error_len)) return 1;
     if (config->sdf_id != FPT_SDF_MANDELBULBER) {
         set_error(error, error_len, "field sampling requires a Mandelbulber scene");
         return 1;
@@ -662,7 +725,12 @@ int fpt_compare_images(const char *baseline_path, const char *candidate_path, co
     if (!baseline_path || !candidate_path || !report_path) { set_error(error, error_len, "missing comparison path"); return 1; }
     Image a, b;
     std::string err;
-    if (!read_png(baseline_path, a, err) || !read_png(candidate_path, b, err)) { set_error(error, error_len, "%s", err.c_str()); return 1; }
+    try {
+        if (!read_png(baseline_path, a, err) || !read_png(candidate_path, b, err)) { set_error(error, error_len, "%s", err.c_str()); return 1; }
+    } catch (const std::exception &ex) {
+        set_error(error, error_len, "failed to read PNG: %s", ex.what());
+        return 1;
+    }
     if (a.width != b.width || a.height != b.height) {
         set_error(error, error_len, "dimension mismatch: baseline %ux%u candidate %ux%u", a.width, a.height, b.width, b.height);
         return 1;
@@ -683,9 +751,9 @@ int fpt_compare_images(const char *baseline_path, const char *candidate_path, co
 
 int fpt_metal_device_name(char *name, size_t name_len) {
     if (!name || name_len == 0) return 1;
-    int dev = 0, count = 0;
-    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) { name[0] = 0; return 1; }
-    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(nullptr, 0)) { name[0] = 0; return 1; }
+    const int dev = ctx().device;
     cudaDeviceProp p;
     if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) { name[0] = 0; return 1; }
     std::snprintf(name, name_len, "%s", p.name);
@@ -723,9 +791,10 @@ int fpt_cuda_render_stats(struct FptCudaRenderStats *stats) {
 int fpt_metal_diagnostic_render(const char *metallib_path, const char *output_path, const char *shader_source,
                                 size_t shader_source_len, const struct FptRenderConfig *config,
                                 const struct FptDiagnosticConfig *diagnostic, double *elapsed_ms, char *error, size_t error_len) {
-    (void)metallib_path; (void)shader_source; (void)shader_source_len;
+    (void)metallib_path;
     if (elapsed_ms) *elapsed_ms = 0.0;
     if (!config || !diagnostic) { set_error(error, error_len, "missing diagnostic render config"); return 1; }
+    if (reject_generated_source(shader_source, shader_source_len, error, error_len)) return 1;
     if (!output_path) { set_error(error, error_len, "missing diagnostic output path"); return 1; }
     if (config->width == 0 || config->height == 0) {
         set_error(error, error_len, "invalid render size %ux%u", config->width, config->height);
@@ -829,6 +898,25 @@ int fpt_test_typed_soa(const char *metallib_path, const struct FptRenderConfig *
     return 0;
 }
 
+int fpt_cuda_set_device(int32_t ordinal) {
+    if (ordinal < 0) return 1;
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    Context &c = ctx();
+    if (c.ready) return ordinal == c.device ? 0 : 1;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || ordinal >= count) return 1;
+    c.device = ordinal;
+    return 0;
+}
+
+int fpt_cuda_get_device(int32_t *ordinal) {
+    if (!ordinal) return 1;
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(nullptr, 0)) { *ordinal = -1; return 1; }
+    *ordinal = ctx().device;
+    return 0;
+}
+
 int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks) {
     std::lock_guard<std::mutex> lock(ctx().mutex);
     ctx().wave_paths = wave_paths;
@@ -837,11 +925,9 @@ int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks) {
 }
 
 int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch) {
-    if (schedule > 1u || batch > 32u) return 1;
+    if (schedule != 0u || batch > 32u) return 1;
     std::lock_guard<std::mutex> lock(ctx().mutex);
-    ctx().march_schedule = schedule;
-    if (schedule == 1u) ctx().ilv_batch = batch;
-    else ctx().refill_batch = batch;
+    ctx().refill_batch = batch;
     return 0;
 }
 

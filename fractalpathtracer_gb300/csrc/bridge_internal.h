@@ -14,6 +14,7 @@ namespace fpt {
 struct Context {
     std::mutex mutex;
     bool ready = false;
+    int device = -1;           // ordinal bound by every entry point (ensure_device)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     DeviceScene *scene = nullptr; size_t cap_scene = 0;
@@ -35,8 +36,6 @@ struct Context {
     // launch tuning (set by the autotuner entry point; 0 = defaults)
     uint32_t wave_paths = 0;   // paths per wave; 0 = min(all paths, 16M)
     int march_blocks = 0;
-    uint32_t march_schedule = 0;   // 0: lockstep, 1: orbit-interleaved (extension formulas)
-    uint32_t ilv_batch = 0;
     uint32_t refill_batch = 0;
     unsigned long long loop_limit_ns = 0;   // persistent-loop time limit of later renders (0: 10 s)
     uint32_t network_engine = 0;   // FPT_CUDA_NET_*: surrogate network on tcgen05 (0) or mma.sync (1)

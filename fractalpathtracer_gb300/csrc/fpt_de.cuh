@@ -409,9 +409,8 @@ template <class T> __device__ __forceinline__ void menger_step(T &x, T &y, T &z,
     dr = dr * T(s);
 }
 
-// The orbit loop as start / step / finish, so a march can run it one
-// iteration at a time (the orbit-interleaved march kernel) with the same
-// arithmetic as orbit_eval.
+// The orbit loop as start / step / finish (orbit_eval runs it to
+// completion).
 template <class T> struct Orbit {
     T x, y, z, dr, r;
     T cx, cy, cz;   // the constant added after each step
@@ -861,35 +860,6 @@ __device__ __forceinline__ Eval ext_eval(const DeviceScene &S, float3 p) {
         if (plane < e.d) { e.d = plane; e.id = 1; }
     }
     return e;
-}
-
-// scene_eval<KIND>(S, p, EV_MAP).d of an extension formula in two halves
-// around its orbit (ext_field, mandel_finish, ground plane, render[6]).
-template <int KIND> __device__ __forceinline__ int ext_eval_begin(const DeviceScene &S, float3 p, Orbit<float> &o) {
-    if (S.sdf_id == FPT_SDF_MANDELBULBER) {
-        float x = p.x, y = p.y, z = p.z;
-        const float ws = fmaxf(S.set_values[0], 1.0f);
-        global_point(S, x, y, z);
-        orbit_start(o, x / ws, z / ws, y / ws);
-    } else {
-        orbit_start(o, p.x, p.y, p.z);
-    }
-    return ext_iterations(S);
-}
-template <int KIND> __device__ __forceinline__ float ext_eval_end(const DeviceScene &S, float3 p, const Orbit<float> &ob) {
-    OrbitResult<float> o = orbit_finish<KIND>(ob);
-    float d;
-    if (S.sdf_id == FPT_SDF_MANDELBULBER) {
-        o.d = o.d * fmaxf(S.set_values[0], 1.0f);
-        d = mandel_finish(S, p, Field4{o.d, o.r, o.dr, o.escaped ? -float(o.iterations) : float(o.iterations)}).d;
-    } else {
-        d = o.d;
-    }
-    if (S.ground_plane) {
-        const float plane = p.y - S.plane_height;
-        if (plane < d) d = plane;
-    }
-    return mixf(d, d / 2.0f, S.render[6]);
 }
 
 // One evaluation of the scene at p.  KIND selects a specialised estimator;

@@ -56,8 +56,6 @@ struct PathLaunch {
     uint64_t *launches;         // host counter of kernel launches, or null
     uint32_t *grids;            // out: blocks of the persistent march and skip grids (2 entries), or null
     unsigned long long loop_limit_ns;   // time limit of the persistent loops (0: 10 s)
-    uint32_t march_schedule;    // 0: lockstep, 1: orbit-interleaved (extension formulas)
-    uint32_t ilv_batch;         // interleaved: lanes that finish together (0: 16)
     uint32_t refill_batch;      // lockstep: finished lanes finish and refill together in groups of this many
 };
 

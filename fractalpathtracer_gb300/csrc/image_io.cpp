@@ -282,6 +282,9 @@ bool read_radiance_hdr(const char *path, HdrImage &out, std::string &err) {
         return false;
     }
     if (!format_ok || width < 8 || width > 32767) { err = std::string("unsupported non-RLE Radiance HDRI ") + path; return false; }
+    // The reference bounds the width only; the height is bounded too, so a
+    // corrupt header cannot ask for more than 32767^2 pixels of floats.
+    if (height > 32767) { err = "HDRI height " + std::to_string(height) + " exceeds 32767 in " + path; return false; }
     out.width = uint32_t(width); out.height = uint32_t(height);
     out.rgb.assign(size_t(width) * height * 3, 0.0f);
     std::vector<uint8_t> scan(size_t(width) * 4);
@@ -327,54 +330,6 @@ bool read_radiance_hdr(const char *path, HdrImage &out, std::string &err) {
     return true;
 }
 
-bool write_radiance_hdr(const char *path, uint32_t w, uint32_t h, const float *rgb, std::string &err) {
-    if (w < 8 || w > 32767) { err = "RGBE width must be in [8, 32767]"; return false; }
-    FILE *f = std::fopen(path, "wb");
-    if (!f) { err = std::string("failed to open ") + path; return false; }
-    std::fprintf(f, "#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y %u +X %u\n", h, w);
-    std::vector<uint8_t> scan(size_t(w) * 4), outb;
-    for (uint32_t y = 0; y < h; ++y) {
-        for (uint32_t x = 0; x < w; ++x) {
-            const float *c = rgb + (size_t(y) * w + x) * 3;
-            float m = std::max(c[0], std::max(c[1], c[2]));
-            uint8_t *s = &scan[size_t(x) * 4];
-            if (!(m > 1e-32f)) { s[0] = s[1] = s[2] = s[3] = 0; continue; }
-            int e;
-            float frac = std::frexp(m, &e);
-            float scale = frac * 256.0f / m;
-            for (int k = 0; k < 3; ++k) s[k] = uint8_t(std::min(255.0f, std::max(0.0f, c[k] * scale)));
-            s[3] = uint8_t(e + 128);
-        }
-        outb.clear();
-        outb.push_back(2); outb.push_back(2); outb.push_back(uint8_t(w >> 8)); outb.push_back(uint8_t(w & 0xff));
-        for (int ch = 0; ch < 4; ++ch) {
-            uint32_t x = 0;
-            while (x < w) {
-                uint32_t run = 1;
-                while (x + run < w && run < 127 && scan[size_t(x + run) * 4 + ch] == scan[size_t(x) * 4 + ch]) ++run;
-                if (run >= 3) {
-                    outb.push_back(uint8_t(128 + run));
-                    outb.push_back(scan[size_t(x) * 4 + ch]);
-                    x += run;
-                } else {
-                    uint32_t start = x, n = 0;
-                    while (x < w && n < 128) {
-                        uint32_t r = 1;
-                        while (x + r < w && r < 3 && scan[size_t(x + r) * 4 + ch] == scan[size_t(x) * 4 + ch]) ++r;
-                        if (r >= 3) break;
-                        ++x; ++n;
-                    }
-                    outb.push_back(uint8_t(n));
-                    for (uint32_t i = 0; i < n; ++i) outb.push_back(scan[size_t(start + i) * 4 + ch]);
-                }
-            }
-        }
-        std::fwrite(outb.data(), 1, outb.size(), f);
-    }
-    bool ok = std::fclose(f) == 0;
-    if (!ok) err = std::string("failed to write ") + path;
-    return ok;
-}
 
 uint16_t reference_float_to_half(float value) {
     uint32_t bits = 0;

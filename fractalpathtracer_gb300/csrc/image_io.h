@@ -24,8 +24,6 @@ struct HdrImage {
 };
 // Radiance RLE reader (src/metal_bridge.mm:2184-2259).
 bool read_radiance_hdr(const char *path, HdrImage &out, std::string &err);
-// Radiance RLE writer (new-style run-length scanlines), the inverse of the reader.
-bool write_radiance_hdr(const char *path, uint32_t w, uint32_t h, const float *rgb, std::string &err);
 // float -> half conversion used by the reference's HDRI LUT (src/metal_bridge.mm:2163-2176).
 uint16_t reference_float_to_half(float value);
 

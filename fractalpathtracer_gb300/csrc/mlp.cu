@@ -656,6 +656,7 @@ int fpt_cuda_mlp_create(const struct FptRenderConfig *config, const struct FptCu
 
 int fpt_cuda_mlp_destroy(uint64_t model) {
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(nullptr, 0)) return 1;
     auto it = mlp::models().find(model);
     if (it == mlp::models().end()) return 1;
     cudaStreamSynchronize(ctx().stream);
@@ -667,6 +668,7 @@ int fpt_cuda_mlp_destroy(uint64_t model) {
 int fpt_cuda_mlp_predict(uint64_t model, const float *points_xyzw, size_t n, float *distances, char *error, size_t error_len) {
     if (!points_xyzw || !distances || n == 0 || n > (size_t(1) << 28)) { set_error(error, error_len, "bad prediction input"); return 1; }
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
     mlp::HostModel *hm = mlp::find(model);
     if (!hm) { set_error(error, error_len, "unknown surrogate model handle"); return 1; }
     Context &c = ctx();
@@ -724,6 +726,7 @@ int fpt_test_bounded_waits(uint32_t *result, size_t result_len, char *error, siz
 
 int fpt_cuda_mlp_get_params(uint64_t model, float *params, size_t len, char *error, size_t error_len) {
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
     mlp::HostModel *hm = mlp::find(model);
     if (!hm) { set_error(error, error_len, "unknown surrogate model handle"); return 1; }
     if (!params || len < size_t(mlp::kParams)) { set_error(error, error_len, "parameter buffer too small (need %d)", mlp::kParams); return 1; }
@@ -735,6 +738,7 @@ int fpt_cuda_mlp_get_params(uint64_t model, float *params, size_t len, char *err
 
 int fpt_cuda_mlp_set_params(uint64_t model, const float *params, size_t len, char *error, size_t error_len) {
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
     mlp::HostModel *hm = mlp::find(model);
     if (!hm) { set_error(error, error_len, "unknown surrogate model handle"); return 1; }
     if (!params || len < size_t(mlp::kParams)) { set_error(error, error_len, "parameter buffer too small (need %d)", mlp::kParams); return 1; }
@@ -753,6 +757,7 @@ int fpt_cuda_mlp_gradients(uint64_t model, const float *points_xyzw, size_t n, f
     if (!points_xyzw || !gradients || n == 0 || n > (size_t(1) << 22)) { set_error(error, error_len, "bad gradient input"); return 1; }
     if (len < size_t(mlp::kParams)) { set_error(error, error_len, "gradient buffer too small (need %d)", mlp::kParams); return 1; }
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
     mlp::HostModel *hm = mlp::find(model);
     if (!hm) { set_error(error, error_len, "unknown surrogate model handle"); return 1; }
     Context &c = ctx();

@@ -47,12 +47,8 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     }
     const bool skip_pass = pl.skip && pl.skip->use_network;
     W.skip_queue = skip_pass ? 1u : 0u;
-    W.ilv_batch = pl.ilv_batch;
     W.refill_batch = pl.refill_batch;
     W.loop_limit_ns = pl.loop_limit_ns ? pl.loop_limit_ns : kLoopLimitNs;
-    // extension formulas can march with the orbit-interleaved kernel (schedule 1)
-    constexpr bool kExt = KIND == KIND_BULB8 || KIND == KIND_BULB || KIND == KIND_BOX || KIND == KIND_MENGER || KIND == KIND_HYBRID;
-    const bool interleaved = kExt && pl.march_schedule == 1u;
     const uint32_t cap = pl.wave_paths;
     char *base = static_cast<char *>(pl.wave_scratch);
     W.paths = reinterpret_cast<PathRec *>(base);
@@ -67,8 +63,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int march_blocks = pl.march_blocks;
     if (march_blocks <= 0) {
-        if (interleaved) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_ilv_kernel<KIND>, 128, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<KIND>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<KIND>, 128, 0);
         march_blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
     const bool skip_tc = skip_pass && pl.skip->engine == kNetTcgen05;
@@ -108,10 +103,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
             // the camera rays only, the box clip applies in every pass.
             if (skip_pass && b == 0u)
                 timed(KC_SKIP, [&] { FPT_CAT(launch_skip_pass_k, FPT_KIND)(W, *pl.skip, skip_tc, skip_blocks, stream); });
-            timed(KC_MARCH, [&] {
-                if (interleaved) march_ilv_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
-                else march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
-            });
+            timed(KC_MARCH, [&] { march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur); });
             if (b < pl.bounces) timed(KC_SHADE, [&] { shade_kernel<KIND><<<shade_blocks, 128, 0, stream>>>(W, cur); });
         }
         finalize_kernel<false><<<(W.n_paths + 255u) / 256u, 256, 0, stream>>>(W);

@@ -684,6 +684,7 @@ int fpt_cuda_voxel_build(const struct FptRenderConfig *config, const struct FptC
 int fpt_cuda_voxel_read(uint32_t *brick_table, size_t table_len, uint8_t *occupancy, uint16_t *distance, uint32_t *cells,
                         size_t cell_len, char *error, size_t error_len) {
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
     VoxelState &V = vstate();
     if (!V.built) { set_error(error, error_len, "no voxel grid has been built"); return 1; }
     size_t nb = size_t(V.brick_grid) * V.brick_grid * V.brick_grid;
@@ -714,6 +715,7 @@ int fpt_cuda_dda_sequence(const float *rays, size_t ray_count, uint32_t capacity
     if (!rays || !hits || ray_count == 0) { set_error(error, error_len, "missing DDA input"); return 1; }
     if (ray_count > 0xffffffffull) { set_error(error, error_len, "too many rays"); return 1; }
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
     Context &c = ctx();
     VoxelState &V = vstate();
     if (!V.built) { set_error(error, error_len, "no voxel grid has been built"); return 1; }
@@ -805,6 +807,7 @@ int fpt_cuda_voxel_render(const struct FptRenderConfig *config, const struct Fpt
     if (hit_count < pixels) { set_error(error, error_len, "hit buffer too small (%zu < %zu)", hit_count, pixels); return 1; }
     if (rgba && rgba_len < pixels * 4) { set_error(error, error_len, "rgba buffer too small"); return 1; }
     std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
     Context &c = ctx();
     VoxelState &V = vstate();
     if (!V.built || V.format != VF_OCCUPANCY) { set_error(error, error_len, "build an occupancy-brick grid first"); return 1; }

@@ -123,7 +123,6 @@ struct WaveParams {
     const uint32_t *pixel_base;  // n_scenes + 1 entries: first pixel of each scene in accum / sample_rgb
     uint32_t n_scenes;
     const uint32_t *pass;        // sample index of the pass (device word, advanced by the pass graph)
-    uint32_t ilv_batch;          // orbit-interleaved march: lanes that finish together (0: 16)
     uint32_t refill_batch;       // lockstep march: finished lanes wait for this many (0: kRefillBatch, 1: none)
     unsigned long long loop_limit_ns;   // time limit of the persistent loops (guard word bit 1 when reached)
 };
@@ -525,186 +524,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
                     atomicMax(W.profile + 12, s);
                 }
             }
-        }
-    }
-}
-
-// Orbit-interleaved march for the extension formulas (march schedule 1).  The
-// lockstep kernel above runs each distance evaluation to completion on every
-// lane, so a warp
-// pays for the longest orbit (evaluations average about 3 of up to 8
-// Mandelbulb iterations, the warp maximum is typically 6-7).  Here a warp trip
-// runs ONE orbit iteration on every lane whose orbit is live; a lane whose
-// orbit ends waits until `batch` lanes (or all live lanes) are ready, then the
-// ready lanes finish the evaluation, take the march step and start their next
-// orbit together.  Same estimator arithmetic (orbit_step / orbit_finish), same
-// march rule, same job queue and outputs as march_kernel.  Measured on the
-// power-8 Mandelbulb at 1080p 16 spp it is slower (48-60 ms of march against
-// 36 ms): the ballots and refill checks of every trip cost more than the idle
-// lanes they save, so lockstep is the default.
-template <int KIND>
-__global__ void __launch_bounds__(128, 7) march_ilv_kernel(WaveParams W, int cur) {
-    const DeviceScene &S = *W.scene;
-    TranslucencyProbe<KIND> probe{W.scene};
-    const uint32_t n_path = W.counters[C_MARCH0 + cur];
-    const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
-    const uint32_t *qm = W.q_march[cur];
-    const ShadowJob *qs = W.q_shadow[cur];
-    const uint32_t lane = threadIdx.x & 31u;
-    const unsigned FULL = 0xffffffffu;
-    const float3 cam = mk3(S.cam_pos[0], S.cam_pos[1], S.cam_pos[2]);
-    const float bailout = ext_bailout(S);
-    const uint32_t batch = W.ilv_batch ? W.ilv_batch : 16u;
-    March m;
-    MarchJob job;
-    Orbit<float> ob;
-    int max_iter = 0;
-    float3 box_origin = mk3(0.0f);
-    float box_exit = 3.0e38f;
-    float known_d = 0.0f;
-    bool have_d = false, live = false;
-    bool active = false, pending = false, retired = false;
-    uint32_t c_primary = 0, c_secondary = 0, c_shadow = 0, c_paths = 0;
-    uint32_t trips = 0;
-    const unsigned long long t0 = global_ns();
-    while (true) {
-        if (loop_guard(trips, t0, W.counters, W.loop_limit_ns)) break;
-        unsigned need = __ballot_sync(FULL, !active && !pending && !retired);
-        if (need) {
-            uint32_t leader = __ffs(need) - 1, base = 0;
-            if (lane == leader) base = atomicAdd(&W.counters[C_HEAD], (unsigned)__popc(need));
-            base = __shfl_sync(FULL, base, leader);
-            if (!active && !pending && !retired) {
-                uint32_t idx = base + __popc(need & ((1u << lane) - 1u));
-                if (idx >= total) {
-                    retired = true;
-                } else if (idx < n_path) {
-                    job.path = qm[idx];
-                    job.shadow = false;
-                    const PathRec &R = W.paths[job.path];
-                    float4 pos = R.pos, dir = R.dir;
-                    uint32_t st = fbits(R.color.w);
-                    job.bounce = st & 0xffu;
-                    int ni = job.bounce == 0u ? int(S.render[1]) : int(S.render[1] / (S.render[5] * 2.0f + 1.0f));
-                    float3 o = mk3(pos.x, pos.y, pos.z), dv = mk3(dir.x, dir.y, dir.z);
-                    float tn = 0.0f, tf = 3.0e38f;
-                    if (W.box_on && !(st & PF_ESCAPED) && !wave_box_span(W, o, dv, tn, tf)) st |= PF_ESCAPED;
-                    if (st & PF_ESCAPED) {
-                        active = false;
-                        m.steps = 0;
-                        m.pos = o + dv * (S.render[4] + len3(o - cam) + 1.0f);
-                    } else {
-                        box_origin = o;
-                        // Leaving the box ends camera rays as misses (their march would end beyond the far limit from
-                        // the camera).  Later path rays keep marching: the reference counts a bounce whose march stops
-                        // within the far limit of the camera as a hit (shaders/Shaders.metal:5971-5976), wherever it
-                        // stops, and the box must not change that.
-                        box_exit = job.bounce == 0u ? tf : 3.0e38f;
-                        // the camera kernel (or the skip pass) placed camera rays; later rays start inside the box
-                        const int before = job.bounce == 0u ? int(R.shadow.w) : 0;
-                        if (before > 0)   // resumes the plain march from the camera (first step s1, or the skip pass's)
-                            active = march_resume(m, S, cam, o, dv, ni, S.render[3], 0.0002f, before,
-                                                  before == 1 ? bitsf(W.counters[C_CAMSTEP]) : 0.0f);
-                        else
-                            active = march_begin(m, S, o, dv, ni, S.render[3], 0.0002f);
-                        have_d = active && (st & PF_KNOWN_D);
-                        known_d = R.grad.w;
-                    }
-                    pending = !active;
-                } else {
-                    const ShadowJob &J = qs[idx - n_path];
-                    float4 o = J.origin, nn = J.normal, d = J.dir;
-                    job.path = fbits(o.w);
-                    job.shadow = true;
-                    job.contrib = J.contrib;
-                    job.rp0 = mk3(o.x, o.y, o.z);
-                    float3 dv = mk3(d.x, d.y, d.z);
-                    float3 start = job.rp0 + mk3(nn.x, nn.y, nn.z) * 0.001f + dv * nn.w;
-                    float tn = 0.0f, tf = 3.0e38f;
-                    const bool miss = d.w == 1.0f || (W.box_on && !wave_box_span(W, start, dv, tn, tf));
-                    if (miss) {
-                        active = false;
-                        m.steps = 0;
-                        m.pos = job.rp0 + dv * (S.render[4] * 1.01f + 1.0f);
-                    } else {
-                        box_origin = start;
-                        box_exit = tf;
-                        active = march_begin(m, S, start, dv, int(S.render[1]), S.render[3], 0.0002f);
-                        have_d = active && d.w == 2.0f;
-                        known_d = J.contrib.w;
-                    }
-                    pending = !active;
-                }
-                live = false;
-                if (active && !have_d) {
-                    max_iter = ext_eval_begin<KIND>(S, m.pos, ob);
-                    live = max_iter > 0;
-                }
-            }
-        }
-        if (!__any_sync(FULL, !retired)) break;
-        // One orbit iteration for every live orbit.
-        if (active && live) live = orbit_step<KIND>(ob, S, max_iter, bailout);
-        // Evaluations whose orbit has ended finish together.
-        const bool ready = active && !live;
-        const unsigned rb = __ballot_sync(FULL, ready), lb = __ballot_sync(FULL, active && live);
-        if (rb && (uint32_t(__popc(rb)) >= batch || lb == 0u)) {
-            if (ready) {
-                const float d = have_d ? known_d : ext_eval_end<KIND>(S, m.pos, ob);
-                have_d = false;
-                active = march_update(m, S, d, probe);
-                if (active && W.box_on && dot(m.pos - box_origin, m.dir) > box_exit) {
-                    active = false;
-                    m.pos = job.shadow ? job.rp0 + m.dir * (S.render[4] * 1.01f + 1.0f)
-                                       : m.pos + m.dir * (S.render[4] + len3(m.pos - cam) + 1.0f);
-                }
-                if (active) {
-                    max_iter = ext_eval_begin<KIND>(S, m.pos, ob);
-                    live = max_iter > 0;
-                }
-                pending = !active;
-            }
-        }
-        if (pending) {
-            pending = false;
-            if (job.shadow) {
-                c_shadow += m.steps;
-                if (len3(job.rp0 - m.pos) > S.render[4] * 0.99f) {
-                    float4 &sh = W.paths[job.path].shadow;
-                    sh = make_float4(sh.x + job.contrib.x, sh.y + job.contrib.y, sh.z + job.contrib.z, sh.w);
-                }
-            } else {
-                if (job.bounce == 0u) c_primary += m.steps; else c_secondary += m.steps;
-                PathRec &R = W.paths[job.path];
-                float3 r = m.pos - cam;
-                float travel2 = dot(r, r);
-                float maxd = S.render[4], far = maxd * 0.99f;
-                bool hit = !(travel2 > far * far);
-                if (job.bounce == 0u && travel2 > maxd * maxd) R.dir.w = 1.0f;
-                if (!hit) {
-                    float4 dir = R.dir;
-                    float3 env = environment(mk3(dir.x, dir.y, dir.z), S);
-                    float4 col = R.color, li = R.light;
-                    if (S.brdf == FPT_CUDA_BRDF_LAMBERT_GGX) env = env * mk3(col.x, col.y, col.z);
-                    R.light = make_float4(li.x + env.x, li.y + env.y, li.z + env.z, li.w);
-                    R.color.w = bitsf(fbits(col.w) | PF_DONE);
-                    c_paths += 1;
-                } else {
-                    R.pos = make_float4(m.pos.x, m.pos.y, m.pos.z, R.pos.w);
-                }
-                uint32_t at = warp_append(&W.counters[C_SHADE], hit);
-                if (hit) W.q_shade[at] = job.path;
-            }
-        }
-    }
-    if (W.profile) {
-        uint32_t v[4] = {c_primary, c_secondary, c_shadow, c_paths};
-        const int slot[4] = {0, 1, 2, 5};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            uint32_t s = v[k];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
-            if (lane == 0 && s) atomicAdd(W.profile + slot[k], (unsigned long long)s);
         }
     }
 }

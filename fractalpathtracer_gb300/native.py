@@ -29,6 +29,7 @@ EXPORTED = [
     "fpt_cuda_set_network_engine",
     "fpt_test_bounded_waits",
     "fpt_cuda_set_loop_limit",
+    "fpt_cuda_set_device", "fpt_cuda_get_device",
 ]
 
 
@@ -74,6 +75,8 @@ def _declare(L: C.CDLL) -> None:
     L.fpt_cuda_render.argtypes = [cfg, ext, C.c_char_p, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_size_t,
                                   P(C.c_double), P(ffi.FptSdfProfileStats)] + err
     L.fpt_cuda_sample_distance.argtypes = [cfg, ext, P(C.c_float), C.c_size_t, P(C.c_float), P(C.c_float)] + err
+    L.fpt_cuda_set_device.argtypes = [C.c_int32]
+    L.fpt_cuda_get_device.argtypes = [P(C.c_int32)]
     for name in EXPORTED:
         getattr(L, name).restype = C.c_int
     _declare_extra(L)
@@ -205,6 +208,18 @@ def compare_images(baseline: str, candidate: str, report: str) -> dict:
         _raise(e)
     with open(report) as f:
         return json.load(f)
+
+
+def set_device(ordinal: int) -> None:
+    """Binds the library's context to a CUDA device (before its first GPU call)."""
+    if lib().fpt_cuda_set_device(int(ordinal)) != 0:
+        raise NativeError(f"cannot bind CUDA device {ordinal} (not visible, or another device is already bound)")
+
+
+def get_device() -> int | None:
+    """Ordinal of the device the library's context is bound to (None without a GPU)."""
+    v = C.c_int32(-1)
+    return v.value if lib().fpt_cuda_get_device(C.byref(v)) == 0 else None
 
 
 def device_name() -> str | None:

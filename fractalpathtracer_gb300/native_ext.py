@@ -340,7 +340,7 @@ def set_network_engine(engine: int = NET_TCGEN05) -> None:
 
 
 def set_march_schedule(schedule: int = 0, batch: int = 0) -> None:
-    """0: lockstep march (default), 1: orbit-interleaved march for the extension formulas."""
+    """Lockstep march (schedule 0, the only one); `batch` finished lanes refill together (0: 8)."""
     from .native import lib
     if lib().fpt_cuda_set_march_schedule(schedule, batch) != 0:
-        raise ValueError("schedule must be 0 or 1 and batch 0..32")
+        raise ValueError("schedule must be 0 and batch 0..32")

@@ -737,8 +737,10 @@ int fpt_cuda_voxel_render(const struct FptRenderConfig *config,
  * brick_size 8.  Scratch lives in one fixed device array of about 2.1 MB
  * that every GPU loading the library holds until the process exits, so the
  * resolution is limited to 512.  The first call on a device looks up that
- * array's device address; make it before any stream capture.  Every call
- * shares the array: calls that overlap on the GPU race. */
+ * array's device address; make it before any stream capture.  The call
+ * returns after the build has finished: it synchronises `stream` to read the
+ * brick count back before the fill, and again at the end.  Every call shares
+ * the array: calls that overlap on the GPU race. */
 int fpt_cuda_voxel_build_static(const struct FptRenderConfig *config,
                                 const struct FptCudaSceneExt *ext,
                                 void *stream,
@@ -855,14 +857,22 @@ int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
  * depend on either. */
 int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks);
 
-/* March schedule of later single-scene renders:
- * 0 lockstep (default; each distance evaluation runs to completion; lanes
- * whose ray finished write it and take the next ray together once `batch` of
- * them wait: 0 = 8, 1 = at once), 1 orbit-interleaved, extension formulas
- * only (one orbit iteration per warp trip; `batch` lanes, 1-32, finish their
- * evaluations together, 0 = 16).  Images agree within FP32
- * rounding; on the power-8 Mandelbulb at 1080p the interleaved march took
- * 48-60 ms against 36 ms for lockstep. */
+/* CUDA device of this process's context (no counterpart in the reference,
+ * which takes the system default Metal device).  The library links its own
+ * CUDA runtime, so the caller's runtime does not choose its device.  Default:
+ * the ordinal in the environment variable FPT_CUDA_DEVICE, else LOCAL_RANK
+ * (one replica per GPU under torchrun), else 0.  fpt_cuda_set_device must come
+ * before the first call that uses the GPU; later it succeeds only for the
+ * device already bound.  Returns 1 for an ordinal that is not visible. */
+int fpt_cuda_set_device(int32_t ordinal);
+/* The ordinal bound by the context (created on first use); 1 without a GPU. */
+int fpt_cuda_get_device(int32_t *ordinal);
+
+/* March schedule of later single-scene renders.  Schedule 0 (the only one)
+ * is lockstep: each distance evaluation runs to completion on every lane, and
+ * lanes whose ray finished write it and take the next ray together once
+ * `batch` of them wait (0 = 8, 1 = at once, at most 32).  Returns 1 for any
+ * other schedule or batch.  Images do not depend on the batch. */
 int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch);
 
 /* Engine of the surrogate network in later skip passes and predictions:

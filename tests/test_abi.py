@@ -106,10 +106,43 @@ def test_settings_validate_arguments_without_gpu(native):
     with pytest.raises(ValueError):
         nx.set_network_engine(7)
     with pytest.raises(ValueError):
-        nx.set_march_schedule(3, 0)
+        nx.set_march_schedule(1, 0)
     with pytest.raises(ValueError):
         nx.set_march_schedule(0, 33)
     nx.set_network_engine(nx.NET_MMA_SYNC)
     nx.set_network_engine(nx.NET_TCGEN05)
     nx.set_march_schedule(0, 0)
     nx.set_loop_limit(0)
+
+
+def test_generated_mandelbulber_source_is_rejected_without_gpu(native):
+    """A shader source generated from a Mandelbulber formula (the generator defines
+    FPT_MANDEL_GENERATED_FIELD, src/mandelbulber/compiler.rs:1510) is refused with
+    a message instead of rendering the built-in formula; the stock source is not."""
+    import ctypes as C
+    lib = native.lib()
+    cfg = ffi.default_config()
+    cfg.width, cfg.height = 4, 4
+    src = b"#include <metal_stdlib>\n#define FPT_MANDEL_GENERATED_FIELD 1\nstatic float4 f();\n"
+    err = C.create_string_buffer(512)
+    rc = lib.fpt_metal_render(b"", b"", b"", b"/nonexistent/out.png", src, len(src), C.byref(cfg), None, None, None, None,
+                              None, None, None, None, None, None, None, None, 0, err, len(err))
+    assert rc == 1 and b"generated Mandelbulber formulas are not supported" in err.value
+    d = ffi.FptDiagnosticConfig()
+    err = C.create_string_buffer(512)
+    rc = lib.fpt_metal_diagnostic_render(b"", b"/nonexistent/d.png", src, len(src), C.byref(cfg), C.byref(d), None, err,
+                                         len(err))
+    assert rc == 1 and b"generated Mandelbulber formulas are not supported" in err.value
+    cfg.sdf_id = ffi.SDF_MANDELBULBER
+    pts = (C.c_float * 4)(0.0, 0.0, 0.0, 1.0)
+    out = ffi.FptMandelbulberFieldSample()
+    err = C.create_string_buffer(512)
+    rc = lib.fpt_mandelbulber_sample_field(b"", src, len(src), C.byref(cfg), pts, 1, C.byref(out), err, len(err))
+    assert rc == 1 and b"generated Mandelbulber formulas are not supported" in err.value
+    # the stock source (what the reference's src/main.rs passes on every other call) passes the check
+    # and fails later, for the missing output path, before touching a GPU
+    stock = b"#include <metal_stdlib>\nkernel void sdf_kernel();\n"
+    err = C.create_string_buffer(512)
+    rc = lib.fpt_metal_render(b"", b"", b"", None, stock, len(stock), C.byref(cfg), None, None, None, None,
+                              None, None, None, None, None, None, None, None, 0, err, len(err))
+    assert rc == 1 and b"missing output path" in err.value
