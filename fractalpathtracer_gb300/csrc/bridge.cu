@@ -152,6 +152,7 @@ static void host_rotate_camera(const float v_in[3], float yaw, float pitch, floa
 uint32_t scene_kind(const FptCudaSceneExt &e) {
     switch (e.formula) {
         case FPT_CUDA_FORMULA_MANDELBULB: return e.power == 8.0f ? KIND_BULB8 : KIND_BULB;
+        case FPT_CUDA_FORMULA_MANDELBULB_POWER2: return KIND_BULB;
         case FPT_CUDA_FORMULA_MANDELBOX: return KIND_BOX;
         case FPT_CUDA_FORMULA_MENGER_FOLD: return KIND_MENGER;
         case FPT_CUDA_FORMULA_BULB_MENGER_HYBRID: return KIND_HYBRID;
@@ -163,7 +164,8 @@ bool compile_scene(const FptRenderConfig &c, const FptCudaSceneExt *ext_in, Devi
     static const FptCudaSceneExt none{};
     const FptCudaSceneExt &e = ext_in ? *ext_in : none;
     std::memset(&S, 0, sizeof(S));
-    if (e.formula != 0 && e.formula != FPT_CUDA_FORMULA_MANDELBULB && e.formula != FPT_CUDA_FORMULA_MANDELBOX &&
+    if (e.formula != 0 && e.formula != FPT_CUDA_FORMULA_MANDELBULB && e.formula != FPT_CUDA_FORMULA_MANDELBULB_POWER2 &&
+        e.formula != FPT_CUDA_FORMULA_MANDELBOX &&
         e.formula != FPT_CUDA_FORMULA_MENGER_FOLD && e.formula != FPT_CUDA_FORMULA_BULB_MENGER_HYBRID) {
         set_error(error, error_len, "unsupported extension formula %u", e.formula);
         return false;
@@ -347,6 +349,27 @@ bool upload_scene(DeviceScene &S, const FptCudaSceneExt *ext, char *error, size_
     }
     if (!ensure_buffer((void **)&c.scene, &c.cap_scene, sizeof(DeviceScene), error, error_len)) return false;
     return check(cudaMemcpyAsync(c.scene, &S, sizeof(DeviceScene), cudaMemcpyHostToDevice, c.stream), "scene upload", error, error_len);
+}
+
+// FP32 fused multiply-add throughput: every thread runs eight independent
+// FMA chains (enough independent work to issue one FMA per cycle on every
+// scheduler), unrolled so the loop adds about one non-FMA instruction per 256
+// FMAs.  Multiplier and addend come from the host, so nothing folds.
+__global__ void __launch_bounds__(256) fma_peak_kernel(float *sink, uint32_t trips, float m, float c) {
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = float(threadIdx.x) * 1.0e-3f + float(k);
+    for (uint32_t i = 0; i < trips; ++i) {
+#pragma unroll 32
+        for (int j = 0; j < 32; ++j) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], m, c);
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == 1.0e30f) sink[0] = s;   // never true: keeps the chains live
 }
 
 }  // namespace fpt
@@ -896,6 +919,54 @@ int fpt_test_typed_soa(const char *metallib_path, const struct FptRenderConfig *
         return 1;
     }
     return 0;
+}
+
+int fpt_cuda_measure_fp32_peak(double *tflops, double *launch_ms, char *error, size_t error_len) {
+    if (tflops) *tflops = 0.0;
+    if (launch_ms) *launch_ms = 0.0;
+    if (!tflops) { set_error(error, error_len, "missing output"); return 1; }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    if (!ensure_buffer((void **)&c.counter, &c.cap_counter, 64, error, error_len)) return 1;
+    int sms = 0;
+    if (!check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device), "SM count", error, error_len)) return 1;
+    const uint32_t blocks = uint32_t(sms) * 8u, threads = 256u, trips = 1024u;   // 2048 threads per SM
+    const double flop = double(blocks) * threads * trips * 32.0 * 8.0 * 2.0;
+    float best = 1e30f;
+    for (int it = 0; it < 8; ++it) {
+        cudaEventRecord(c.ev0, c.stream);
+        fma_peak_kernel<<<blocks, threads, 0, c.stream>>>(reinterpret_cast<float *>(c.counter), trips, 0.99999f, 1.0e-6f);
+        cudaEventRecord(c.ev1, c.stream);
+        if (!check(cudaEventSynchronize(c.ev1), "FP32 peak kernel", error, error_len)) return 1;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        if (it >= 2) best = std::min(best, ms);   // two warm-up launches
+    }
+    if (!check(cudaGetLastError(), "FP32 peak launch", error, error_len)) return 1;
+    *tflops = flop / (double(best) * 1e-3) / 1e12;
+    if (launch_ms) *launch_ms = best;
+    return 0;
+}
+
+int fpt_cuda_hdri_lut(const char *hdri_path, uint16_t *lut, size_t lut_len, char *error, size_t error_len) {
+    const size_t n = size_t(FPT_HDRI_LUT_WIDTH) * FPT_HDRI_LUT_HEIGHT * 3;
+    if (!hdri_path || !lut || lut_len < n) { set_error(error, error_len, "missing HDRI path or LUT buffer (%zu halves)", n); return 1; }
+    const size_t len = std::strlen(hdri_path);
+    FptRenderConfig *cfg = new (std::nothrow) FptRenderConfig();
+    if (!cfg) { set_error(error, error_len, "out of host memory"); return 1; }
+    if (len >= sizeof(cfg->hdri_path)) {
+        delete cfg;
+        set_error(error, error_len, "HDRI path longer than %zu bytes", sizeof(cfg->hdri_path) - 1);
+        return 1;
+    }
+    std::memcpy(cfg->hdri_path, hdri_path, len + 1);
+    cfg->hdri_enabled = 1u;
+    cfg->world[0] = 2.0f;
+    const bool ok = hydrate_hdri(*cfg, error, error_len);
+    if (ok) std::memcpy(lut, cfg->hdri_lut, n * sizeof(uint16_t));
+    delete cfg;
+    return ok ? 0 : 1;
 }
 
 int fpt_cuda_set_device(int32_t ordinal) {

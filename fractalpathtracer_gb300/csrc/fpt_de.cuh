@@ -375,6 +375,20 @@ __device__ __forceinline__ void bulb_step(float &x, float &y, float &z, float &d
     y = ct * sp * rp;
     z = st * rp;
 }
+// Quadratic triplex, Mandelbulber formula 3 (orbit.rs:752-764): the
+// derivative doubles by r with no +1.  On the z axis the division makes the
+// point non-finite and the orbit loop rolls the step back.
+template <class T> __device__ __forceinline__ void triplex2_step(T &x, T &y, T &z, T &dr, T r) {
+    dr = dr * (T(2.0f) * r);
+    const T x2 = x * x, y2 = y * y, z2 = z * z;
+    const T rho2 = x2 + y2;
+    const T temp = T(1.0f) - z2 / rho2;
+    const T nx = (x2 - y2) * temp;
+    const T ny = T(2.0f) * x * y * temp;
+    z = T(-2.0f) * z * s_sqrt(rho2);
+    x = nx;
+    y = ny;
+}
 // Mandelbox step (orbit.rs:1636-1693, no rotations, zero offset).
 template <class T> __device__ __forceinline__ void box_step(T &x, T &y, T &z, T &dr, const DeviceScene &S) {
     const float lim = S.box_fold_limit, val = S.box_fold_value;
@@ -435,8 +449,10 @@ __device__ __forceinline__ bool orbit_step(Orbit<T> &o, const DeviceScene &S, in
     const int i = o.i;
     bool add_c = true;
     if (KIND == KIND_BULB8) bulb8_step(o.x, o.y, o.z, o.dr, o.r);
-    else if (KIND == KIND_BULB) bulb_step(o.x, o.y, o.z, o.dr, o.r, S.power);
-    else if (KIND == KIND_BOX) box_step(o.x, o.y, o.z, o.dr, S);
+    else if (KIND == KIND_BULB) {
+        if (S.formula == FPT_CUDA_FORMULA_MANDELBULB_POWER2) triplex2_step(o.x, o.y, o.z, o.dr, o.r);
+        else bulb_step(o.x, o.y, o.z, o.dr, o.r, S.power);
+    } else if (KIND == KIND_BOX) box_step(o.x, o.y, o.z, o.dr, S);
     else if (KIND == KIND_MENGER) { menger_step(o.x, o.y, o.z, o.dr, S.menger_scale); add_c = false; }
     else {  // KIND_HYBRID
         const int period = S.hybrid_period > 1u ? int(S.hybrid_period) : 3;

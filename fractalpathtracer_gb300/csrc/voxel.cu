@@ -240,6 +240,24 @@ __device__ __forceinline__ float3 offset_origin(float3 pos, float3 n, float3 dir
     float side = (dir.x * n.x + dir.y * n.y + dir.z * n.z) >= 0.0f ? 1.0f : -1.0f;
     return make_float3(pos.x + n.x * side * eps, pos.y + n.y * side * eps, pos.z + n.z * side * eps);
 }
+// offsetVoxelRayOrigin in either mode: legacy (a hundredth of the smallest
+// cell edge along the directed normal) or precision (precisionOffsetRayOrigin,
+// shaders/Shaders.metal:4057-4072: 256 representable floats along the normal,
+// an absolute 2^-16 step within 1/32 of zero).
+__device__ __forceinline__ float3 offset_origin_mode(float3 pos, float3 n, float3 dir, float eps, uint32_t mode) {
+    if (mode != FPT_VOXEL_OFFSET_PRECISION) return offset_origin(pos, n, dir, eps);
+    const float side = (dir.x * n.x + dir.y * n.y + dir.z * n.z) >= 0.0f ? 1.0f : -1.0f;
+    const float dn[3] = {n.x * side, n.y * side, n.z * side}, p[3] = {pos.x, pos.y, pos.z};
+    float r[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int off = int(256.0f * dn[a]);
+        int bits = __float_as_int(p[a]);
+        bits += p[a] < 0.0f ? -off : off;
+        r[a] = fabsf(p[a]) < 1.0f / 32.0f ? p[a] + (1.0f / 65536.0f) * dn[a] : __int_as_float(bits);
+    }
+    return make_float3(r[0], r[1], r[2]);
+}
 
 // Primary + one shadow ray per pixel through the occupancy-brick grid.
 __global__ void __launch_bounds__(128) voxel_primary_kernel(vox::Grid g, CamExact C, uint32_t W, uint32_t H, float3 sun,
@@ -301,7 +319,7 @@ __global__ void __launch_bounds__(128) dda_sequence_kernel(vox::Grid g, const fl
 __device__ float3 voxel_env(const DeviceScene &S, float3 d) { return environment(d, S); }
 
 __global__ void __launch_bounds__(128) voxel_path_kernel(const DeviceScene *scene, vox::Grid g, float4 *accum, uint32_t sample_begin,
-                                                         uint32_t sample_end) {
+                                                         uint32_t sample_end, uint32_t offset_mode) {
     const DeviceScene &S = *scene;
     uint32_t gx = blockIdx.x * 16u + (threadIdx.x & 15u), gy = blockIdx.y * 8u + (threadIdx.x >> 4);
     if (gx >= S.width || gy >= S.height) return;
@@ -358,7 +376,7 @@ __global__ void __launch_bounds__(128) voxel_path_kernel(const DeviceScene *scen
                 sincosf(a1 * 2.0f * kPi, &sa, &ca);
                 float ss = sqrtf(a2) * S.sun[4];
                 ld = rotate_camera(ld, ca * ss, sa * ss);
-                float3 so = offset_origin(hp, nrm, ld, eps);
+                float3 so = offset_origin_mode(hp, nrm, ld, eps, offset_mode);
                 vox::Hit sh = vox::trace(g, so, ld, nullptr, 0, nullptr, nullptr);
                 if (!sh.hit)
                     light = light + mk3(S.sun_color[0], S.sun_color[1], S.sun_color[2]) *
@@ -391,7 +409,7 @@ __global__ void __launch_bounds__(128) voxel_path_kernel(const DeviceScene *scen
                     transmitted = true;
                 }
             }
-            pos = transmitted ? hp + dir * (cell * 1.05f) : offset_origin(hp, nrm, dir, eps);
+            pos = transmitted ? hp + dir * (cell * 1.05f) : offset_origin_mode(hp, nrm, dir, eps, offset_mode);
             if (S.russian_roulette != 0u && bounce + 1 < int(S.bounces) && float(bounce + 1) >= S.rr_start) {
                 float surv = clampf(maxc3(color), clampf(S.rr_min_prob, 0.01f, 1.0f), 1.0f);
                 if (rng.uniform(SLOT_RR, bounce) > surv) break;
@@ -537,6 +555,11 @@ static bool build_grid(const FptRenderConfig &config, const FptCudaSceneExt *ext
     VoxelState &V = vstate();
     uint32_t res = config.voxel_resolution;
     if (res == 0 || res > 4096) { set_error(error, error_len, "voxel resolution %u out of range (1..4096)", res); return false; }
+    if (config.voxel_coverage_mode != FPT_VOXEL_COVERAGE_LEGACY) {
+        set_error(error, error_len, "voxel coverage mode %u (certified program bounds) is not supported by the CUDA path",
+                  config.voxel_coverage_mode);
+        return false;
+    }
     if (brick_size != 0 && brick_size != 4 && brick_size != 8) { set_error(error, error_len, "brick size must be 4 or 8"); return false; }
     for (int k = 0; k < 3; ++k) {
         if (!(config.voxel_bounds_max[k] > config.voxel_bounds_min[k])) {
@@ -618,6 +641,26 @@ int voxel_render_core(const FptRenderConfig &config, const FptCudaSceneExt *ext,
         set_error(error, error_len, "template-brick voxel storage is not supported by the CUDA path");
         return 1;
     }
+    // renderVoxelPath modes the CUDA path does not restate fail loudly instead
+    // of rendering with the defaults.
+    if (config.voxel_normal_mode != FPT_VOXEL_NORMAL_FACE) {
+        set_error(error, error_len, "voxel normal mode %u (smooth / exact field normals) is not supported by the CUDA path",
+                  config.voxel_normal_mode);
+        return 1;
+    }
+    if (config.voxel_material_mode != FPT_VOXEL_MATERIAL_STORED) {
+        set_error(error, error_len, "voxel material mode %u (exact materials) is not supported by the CUDA path",
+                  config.voxel_material_mode);
+        return 1;
+    }
+    if (config.voxel_leaf_refinement != FPT_VOXEL_LEAF_REFINEMENT_NONE) {
+        set_error(error, error_len, "voxel leaf refinement %u is not supported by the CUDA path", config.voxel_leaf_refinement);
+        return 1;
+    }
+    if (config.voxel_offset_mode != FPT_VOXEL_OFFSET_LEGACY && config.voxel_offset_mode != FPT_VOXEL_OFFSET_PRECISION) {
+        set_error(error, error_len, "unknown voxel offset mode %u", config.voxel_offset_mode);
+        return 1;
+    }
     uint32_t bs = config.voxel_storage == FPT_VOXEL_STORAGE_DENSE ? 0u : 4u;
     if (!build_grid(config, ext, S, bs, build_ms, error, error_len)) return 1;
     VoxelState &V = vstate();
@@ -635,7 +678,8 @@ int voxel_render_core(const FptRenderConfig &config, const FptCudaSceneExt *ext,
                               ? std::min(std::max(config.sdf_chunk_samples, 1u), 64u)
                               : (config.sdf_accumulation_mode == FPT_SDF_ACCUMULATION_PER_SAMPLE ? 1u : spp);
     for (uint32_t s0 = 0; s0 < spp; s0 += step)
-        voxel_path_kernel<<<grid, 128, 0, c.stream>>>(c.scene, grid_view(), c.accum, s0, std::min(spp, s0 + step));
+        voxel_path_kernel<<<grid, 128, 0, c.stream>>>(c.scene, grid_view(), c.accum, s0, std::min(spp, s0 + step),
+                                                       config.voxel_offset_mode);
     if (!check(launch_present(c.scene, S.width, S.height, c.accum, c.rgba, c.stream), "present launch", error, error_len)) return 1;
     cudaEventRecord(c.ev1, c.stream);
     if (!check(cudaStreamSynchronize(c.stream), "voxel render", error, error_len)) return 1;

@@ -37,6 +37,7 @@ VOXEL_BUILD_STAGING, VOXEL_BUILD_DIRECT = 0, 1
 
 FORMULA_REFERENCE = 0
 FORMULA_MANDELBULB = 2
+FORMULA_MANDELBULB_POWER2 = 3
 FORMULA_MANDELBOX = 8
 FORMULA_MENGER_FOLD = 100
 FORMULA_BULB_MENGER_HYBRID = 101

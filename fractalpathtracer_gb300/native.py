@@ -29,7 +29,8 @@ EXPORTED = [
     "fpt_cuda_set_network_engine",
     "fpt_test_bounded_waits",
     "fpt_cuda_set_loop_limit",
-    "fpt_cuda_set_device", "fpt_cuda_get_device",
+    "fpt_cuda_set_device", "fpt_cuda_get_device", "fpt_cuda_hdri_lut",
+    "fpt_cuda_measure_fp32_peak",
 ]
 
 
@@ -76,6 +77,8 @@ def _declare(L: C.CDLL) -> None:
                                   P(C.c_double), P(ffi.FptSdfProfileStats)] + err
     L.fpt_cuda_sample_distance.argtypes = [cfg, ext, P(C.c_float), C.c_size_t, P(C.c_float), P(C.c_float)] + err
     L.fpt_cuda_set_device.argtypes = [C.c_int32]
+    L.fpt_cuda_hdri_lut.argtypes = [C.c_char_p, P(C.c_uint16), C.c_size_t] + err
+    L.fpt_cuda_measure_fp32_peak.argtypes = [P(C.c_double), P(C.c_double)] + err
     L.fpt_cuda_get_device.argtypes = [P(C.c_int32)]
     for name in EXPORTED:
         getattr(L, name).restype = C.c_int
@@ -208,6 +211,24 @@ def compare_images(baseline: str, candidate: str, report: str) -> dict:
         _raise(e)
     with open(report) as f:
         return json.load(f)
+
+
+def measure_fp32_peak() -> dict:
+    """FP32 FMA throughput of the library's device (TFLOP/s) and the best launch time (ms)."""
+    t, ms = C.c_double(), C.c_double()
+    e = _err()
+    if lib().fpt_cuda_measure_fp32_peak(C.byref(t), C.byref(ms), e, len(e)) != 0:
+        _raise(e)
+    return {"tflops": t.value, "launch_ms": ms.value}
+
+
+def hdri_lut(path: str) -> np.ndarray:
+    """The 32x16x3 FP16 LUT (bits) a world-mode-2 render builds from the .hdr at `path` (host code)."""
+    lut = np.zeros(32 * 16 * 3, np.uint16)
+    e = _err()
+    if lib().fpt_cuda_hdri_lut(_b(path), _ptr(lut, C.c_uint16), lut.size, e, len(e)) != 0:
+        _raise(e)
+    return lut
 
 
 def set_device(ordinal: int) -> None:

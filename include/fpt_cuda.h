@@ -544,12 +544,14 @@ int fpt_metal_preview(const char *metallib_path,
 /* ------------------------------------------------------------------------- */
 
 /* Formula selected by FptCudaSceneExt.formula.  0 keeps the reference
- * scene of FptRenderConfig.sdf_id.  2 and 8 follow Mandelbulber's formula
- * numbering and the FP64 orbit code of src/mandelbulber/orbit.rs
- * (mandelbulb 766-778, mandelbox 1636-1693, finalizers 638-683). */
+ * scene of FptRenderConfig.sdf_id.  2, 3 and 8 follow Mandelbulber's formula
+ * numbering (src/mandelbulber.rs:1414-1425) and the FP64 orbit code of
+ * src/mandelbulber/orbit.rs (mandelbulb 766-778, quadratic triplex
+ * "mandelbulb power 2" 752-764, mandelbox 1636-1693, finalizers 638-683). */
 enum {
     FPT_CUDA_FORMULA_REFERENCE = 0,
     FPT_CUDA_FORMULA_MANDELBULB = 2,
+    FPT_CUDA_FORMULA_MANDELBULB_POWER2 = 3,
     FPT_CUDA_FORMULA_MANDELBOX = 8,
     FPT_CUDA_FORMULA_MENGER_FOLD = 100,
     FPT_CUDA_FORMULA_BULB_MENGER_HYBRID = 101,
@@ -856,6 +858,21 @@ int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
  * persistent march grid (0: one wave of resident blocks).  Results do not
  * depend on either. */
 int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks);
+
+/* Measured FP32 throughput of this device: a kernel of independent FMA chains
+ * (2048 threads per SM) timed with CUDA events, best of six launches after two
+ * warm-ups, about 2 ms each.  tflops = 2 x FMAs / time; launch_ms (optional)
+ * the best launch.  No counterpart in the reference; it is the denominator of
+ * the FP32 roofline the benchmark reports for the march kernel.  Changes no
+ * clock or other device setting. */
+int fpt_cuda_measure_fp32_peak(double *tflops, double *launch_ms, char *error, size_t error_len);
+
+/* The 32x16 FP16 environment LUT that a render in world mode 2 samples,
+ * built from a Radiance .hdr file exactly as the bridge hydrates
+ * FptRenderConfig.hdri_lut before every render (src/metal_bridge.mm:2262-2300).
+ * No counterpart in the reference, where hydration is internal; host only.
+ * lut gets 32*16*3 halves (lut_len at least that). */
+int fpt_cuda_hdri_lut(const char *hdri_path, uint16_t *lut, size_t lut_len, char *error, size_t error_len);
 
 /* CUDA device of this process's context (no counterpart in the reference,
  * which takes the system default Metal device).  The library links its own

@@ -32,6 +32,7 @@ def lib() -> C.CDLL:
         L.oracle_focus_distance.argtypes = [vp, vp, C.c_int]
         L.oracle_focus_distance.restype = C.c_double
         L.oracle_render.argtypes = [vp, vp, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_float), P(C.c_double)]
+        L.oracle_render_grid.argtypes = [vp, vp, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_float), P(C.c_double)]
         L.oracle_render_path.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, P(C.c_float)]
         L.oracle_present.argtypes = [vp, P(C.c_float), P(C.c_uint8)]
         L.oracle_image_metrics.argtypes = [P(C.c_uint8), P(C.c_uint8), C.c_uint32, C.c_uint32, P(C.c_double)]
@@ -42,7 +43,11 @@ def lib() -> C.CDLL:
         L.oracle_dda.argtypes = [vp, C.c_uint32, P(C.c_uint32), P(C.c_uint8), P(C.c_uint32), P(C.c_float), C.c_size_t,
                                  C.c_uint32, P(C.c_uint32), P(C.c_uint32), P(C.c_double)]
         L.oracle_voxel_primary.argtypes = [vp, vp, P(C.c_uint32), P(C.c_uint8), C.c_uint32, C.c_uint32, P(C.c_double)]
+        L.oracle_voxel_render.argtypes = [vp, vp, C.c_uint32, P(C.c_uint32), P(C.c_uint32), C.c_uint32, C.c_uint32,
+                                          P(C.c_float)]
         L.oracle_dda_contract.restype = C.c_uint32
+        L.oracle_hdri_lut.argtypes = [C.c_char_p, P(C.c_uint16), C.c_char_p, C.c_size_t]
+        L.oracle_hdri_lut.restype = C.c_int
         L.oracle_float_to_half.argtypes = [C.c_float]
         L.oracle_float_to_half.restype = C.c_uint16
         fp = P(C.c_float)
@@ -86,7 +91,8 @@ def field_sample(cfg, ext, points, fp64=True):
 
 
 def orbit_step(ext, point4, iterations=1, bailout=1e300, add_c=False):
-    out = np.zeros(9, np.float64)
+    """{x, y, z, w, dr, r, iterations, escaped, distance, colour} after `iterations` formula steps."""
+    out = np.zeros(10, np.float64)
     p = np.ascontiguousarray(point4, np.float64)
     lib().oracle_orbit_step(_ref(ext), p.ctypes.data_as(C.POINTER(C.c_double)), iterations, bailout, int(add_c),
                             out.ctypes.data_as(C.POINTER(C.c_double)))
@@ -112,6 +118,16 @@ def render(cfg, ext, rows=None, x_stride=1, fp64=False):
     stats = np.zeros(4, np.float64)
     lib().oracle_render(_ref(cfg), _ref(ext), int(fp64), y0, y1, x_stride, acc.ctypes.data_as(C.POINTER(C.c_float)),
                         stats.ctypes.data_as(C.POINTER(C.c_double)))
+    return acc, stats[0]
+
+
+def render_grid(cfg, ext, y_stride, x_stride, fp64=False):
+    """Batch accumulation of every y_stride-th row and x_stride-th column (a sample spread evenly over the
+    frame): (H, W, 4) float32 with only those pixels filled, and the evaluation count."""
+    acc = np.zeros((cfg.height, cfg.width, 4), np.float32)
+    stats = np.zeros(4, np.float64)
+    lib().oracle_render_grid(_ref(cfg), _ref(ext), int(fp64), 0, cfg.height, y_stride, x_stride,
+                             acc.ctypes.data_as(C.POINTER(C.c_float)), stats.ctypes.data_as(C.POINTER(C.c_double)))
     return acc, stats[0]
 
 
@@ -178,6 +194,27 @@ def voxel_primary(cfg, ext, table, occ, rows=None):
     out = np.zeros((cfg.height, cfg.width, 5), np.float64)
     lib().oracle_voxel_primary(_ref(cfg), _ref(ext), _p(table, C.c_uint32), _p(occ, C.c_uint8), y0, y1, _p(out, C.c_double))
     return out
+
+
+def voxel_render(cfg, ext, table, cells, brick_size=4, rows=None):
+    """renderVoxelPath accumulated over the config's samples for rows [y0, y1) through reference cells
+    (brick_size 4 with a page table, 0 dense): (H, W, 4) float32, row 0 at the bottom."""
+    y0, y1 = rows if rows is not None else (0, cfg.height)
+    acc = np.zeros((cfg.height, cfg.width, 4), np.float32)
+    t = np.ascontiguousarray(table, np.uint32) if table is not None else None
+    c = np.ascontiguousarray(cells, np.uint32)
+    lib().oracle_voxel_render(_ref(cfg), _ref(ext), brick_size, _p(t, C.c_uint32), _p(c, C.c_uint32), y0, y1,
+                              _p(acc, C.c_float))
+    return acc
+
+
+def hdri_lut(path):
+    """The reference's 32x16x3 FP16 LUT (bits) of a Radiance .hdr file."""
+    lut = np.zeros(32 * 16 * 3, np.uint16)
+    err = C.create_string_buffer(256)
+    if lib().oracle_hdri_lut(path.encode(), _p(lut, C.c_uint16), err, len(err)) != 0:
+        raise ValueError(err.value.decode())
+    return lut
 
 
 def dda_contract():

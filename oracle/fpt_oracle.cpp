@@ -454,13 +454,30 @@ template <class T> inline void stepMandelbulb(T z[4], T &dr, T r, double power) 
     z[1] = ct * std::sin(phi) * rp;
     z[2] = std::sin(theta) * rp;
 }
+// orbit.rs:752-764 (quadratic triplex, Mandelbulber formula 3): no +1 in the
+// derivative; on the z axis the division gives a non-finite point, which the
+// orbit loop rolls back.
+template <class T> inline void stepMandelbulbPower2(T z[4], T &dr, T r) {
+    dr = dr * (T(2) * r);
+    T x2 = z[0] * z[0], y2 = z[1] * z[1], z2 = z[2] * z[2];
+    T temp = T(1) - z2 / (x2 + y2);
+    T x = (x2 - y2) * temp;
+    T y = T(2) * z[0] * z[1] * temp;
+    T zz = T(-2) * z[2] * std::sqrt(x2 + y2);
+    z[0] = x; z[1] = y; z[2] = zz;
+}
+// Colour increments of the Mandelbox: per folded axis, and for the minimum /
+// fixed radius spheres (Mandelbulber's defaults, the parameters of the
+// reference's own test at orbit.rs:1946-1948).
+constexpr double kBoxColorFactor[3] = {0.03, 0.05, 0.07};
+constexpr double kBoxColorSphereMin = 0.2, kBoxColorSphereFixed = 0.2;
 // orbit.rs:1636-1693 (full Mandelbox, rotations disabled, zero offset).
 template <class T> inline void stepMandelbox(T z[4], T &dr, T &color, const Ext &e) {
     T limit = T(e.box_fold_limit), value = T(e.box_fold_value);
     for (int a = 0; a < 3; ++a) {
         if (std::fabs(z[a]) > limit) {
             z[a] = signv(z[a]) * value - z[a];
-            color += T(0.0);
+            color += T(kBoxColorFactor[a]);
         }
     }
     T r2 = z[0] * z[0] + z[1] * z[1] + z[2] * z[2] + z[3] * z[3];
@@ -470,10 +487,12 @@ template <class T> inline void stepMandelbox(T z[4], T &dr, T &color, const Ext 
         T f = fixed2 / min2;
         for (int k = 0; k < 4; ++k) z[k] = z[k] * f;
         dr = dr * f;
+        color += T(kBoxColorSphereMin);
     } else if (r2 < fixed2) {
         T f = fixed2 / r2;
         for (int k = 0; k < 4; ++k) z[k] = z[k] * f;
         dr = dr * f;
+        color += T(kBoxColorSphereFixed);
     }
     T s = T(e.box_scale);
     for (int k = 0; k < 4; ++k) z[k] = z[k] * s;
@@ -508,6 +527,7 @@ template <class T> OrbitOut<T> orbitEval(const Ext &e, int max_iter, double bail
         bool add_c = true;
         switch (e.formula) {
             case FPT_CUDA_FORMULA_MANDELBULB: stepMandelbulb(z, dr, r, double(e.power)); break;
+            case FPT_CUDA_FORMULA_MANDELBULB_POWER2: stepMandelbulbPower2(z, dr, r); break;
             case FPT_CUDA_FORMULA_MANDELBOX: stepMandelbox(z, dr, color, e); break;
             case FPT_CUDA_FORMULA_MENGER_FOLD: stepMenger(z, dr, T(e.menger_scale)); add_c = false; break;
             case FPT_CUDA_FORMULA_BULB_MENGER_HYBRID:
@@ -1578,17 +1598,18 @@ template <class T> void trace_primary_impl(const Cfg &c, const Ext &e, uint32_t 
     }
 }
 
-template <class T> void render_impl(const Cfg &c, const Ext &e, uint32_t y0, uint32_t y1, uint32_t x_stride, float *accum,
-                                    double *stats) {
+template <class T> void render_impl(const Cfg &c, const Ext &e, uint32_t y0, uint32_t y1, uint32_t y_stride, uint32_t x_stride,
+                                    float *accum, double *stats) {
     T focus = c.focus_distance > 0.0f ? T(c.focus_distance) : estimateFocus<T>(c, e);
     uint32_t samples = std::min(std::max(c.samples, 1u), 512u);
     const long long W = c.width;
     const long long cols = (W + x_stride - 1) / x_stride;
-    const long long total = (long long)(y1 - y0) * cols;
+    const long long rows = (long long)(y1 - y0 + y_stride - 1) / y_stride;
+    const long long total = rows * cols;
     long long steps = 0;
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : steps)
     for (long long k = 0; k < total; ++k) {
-        uint32_t gy = y0 + uint32_t(k / cols), gx = uint32_t((k % cols) * x_stride);
+        uint32_t gy = y0 + uint32_t(k / cols) * y_stride, gx = uint32_t((k % cols) * x_stride);
         V2<float> uv = screenUv(gx, gy, c);
         uint32_t pixel = gy * c.width + gx;
         V3<T> col(T(0));
@@ -1648,7 +1669,7 @@ void oracle_field_sample(const FptRenderConfig *c, const FptCudaSceneExt *e, con
 }
 
 // Orbit formula alone (no world transform): the known-answer hook for
-// src/mandelbulber/orbit.rs:1866-1960.  out = {x, y, z, w, dr, r, iterations, escaped, distance}.
+// src/mandelbulber/orbit.rs:1866-1960.  out = {x, y, z, w, dr, r, iterations, escaped, distance, colour}.
 void oracle_orbit_step(const FptCudaSceneExt *e, const double *p4, int iterations, double bailout, int add_c, double *out) {
     Ext ex = *e;
     double z[4] = {p4[0], p4[1], p4[2], p4[3]};
@@ -1660,6 +1681,7 @@ void oracle_orbit_step(const FptCudaSceneExt *e, const double *p4, int iteration
     for (int i = 0; i < iterations; ++i) {
         switch (ex.formula) {
             case FPT_CUDA_FORMULA_MANDELBULB: stepMandelbulb(z, dr, r, double(ex.power)); break;
+            case FPT_CUDA_FORMULA_MANDELBULB_POWER2: stepMandelbulbPower2(z, dr, r); break;
             case FPT_CUDA_FORMULA_MANDELBOX: stepMandelbox(z, dr, color, ex); break;
             case FPT_CUDA_FORMULA_MENGER_FOLD: stepMenger(z, dr, double(ex.menger_scale)); break;
             default: break;
@@ -1673,6 +1695,7 @@ void oracle_orbit_step(const FptCudaSceneExt *e, const double *p4, int iteration
     out[4] = dr; out[5] = r; out[6] = it; out[7] = esc ? 1 : 0;
     OrbitOut<double> o = orbitEval(ex, iterations, bailout, V3<double>(p4[0], p4[1], p4[2]));
     out[8] = o.d;
+    out[9] = color;
 }
 
 // Per-pixel primary march; out has width*height*6 doubles
@@ -1692,8 +1715,18 @@ double oracle_focus_distance(const FptRenderConfig *c, const FptCudaSceneExt *e,
 void oracle_render(const FptRenderConfig *c, const FptCudaSceneExt *e, int fp64, uint32_t y0, uint32_t y1, uint32_t x_stride,
                    float *accum, double *stats) {
     if (x_stride == 0) x_stride = 1;
-    if (fp64) render_impl<double>(*c, ext_or_default(e), y0, y1, x_stride, accum, stats);
-    else render_impl<float>(*c, ext_or_default(e), y0, y1, x_stride, accum, stats);
+    if (fp64) render_impl<double>(*c, ext_or_default(e), y0, y1, 1u, x_stride, accum, stats);
+    else render_impl<float>(*c, ext_or_default(e), y0, y1, 1u, x_stride, accum, stats);
+}
+
+// Every y_stride-th row of [y0, y1) and every x_stride-th pixel of those rows:
+// a sample spread evenly over the frame.
+void oracle_render_grid(const FptRenderConfig *c, const FptCudaSceneExt *e, int fp64, uint32_t y0, uint32_t y1, uint32_t y_stride,
+                        uint32_t x_stride, float *accum, double *stats) {
+    if (x_stride == 0) x_stride = 1;
+    if (y_stride == 0) y_stride = 1;
+    if (fp64) render_impl<double>(*c, ext_or_default(e), y0, y1, y_stride, x_stride, accum, stats);
+    else render_impl<float>(*c, ext_or_default(e), y0, y1, y_stride, x_stride, accum, stats);
 }
 
 // One path sample (debug hook): rgb out.
@@ -1931,9 +1964,9 @@ inline bool occupied(const VGrid &g, const int c[3], uint32_t &payload) {
     if (g.storage == 4u) return g.occ[payload] != 0u;
     return (g.cells[size_t(payload) * 3] & 0x80000000u) != 0u;
 }
-struct VHit { bool hit; float t; int cell[3]; V3<float> normal; uint32_t steps; };
+struct VHit { bool hit; float t; int cell[3]; V3<float> normal; uint32_t steps; uint32_t payload; };
 inline VHit trace(const VGrid &g, V3<float> o, V3<float> d, std::vector<uint32_t> *seq) {
-    VHit h{false, kInf, {0, 0, 0}, V3<float>(0.f), 0u};
+    VHit h{false, kInf, {0, 0, 0}, V3<float>(0.f), 0u, 0u};
     float near_t, far_t;
     V3<float> en;
     if (!ray_aabb(o, d, g.bmin, g.bmax, near_t, far_t, en)) return h;
@@ -1967,11 +2000,121 @@ inline VHit trace(const VGrid &g, V3<float> o, V3<float> d, std::vector<uint32_t
         uint32_t payload = 0;
         if (occupied(g, c, payload)) {
             h.hit = true; h.t = et; h.cell[0] = c[0]; h.cell[1] = c[1]; h.cell[2] = c[2]; h.normal = en; h.steps = s + 1;
+            h.payload = payload;
             return h;
         }
         if (!advance(c, st, nt, dt, et, en)) break;
     }
     return h;
+}
+
+// offsetVoxelRayOrigin and precisionOffsetRayOrigin (shaders/Shaders.metal:4057-4090).
+inline V3<float> voxel_offset_origin(V3<float> pos, V3<float> n, V3<float> dir, const Cfg &c, float eps) {
+    const float side = dot(dir, n) >= 0.0f ? 1.0f : -1.0f;
+    const V3<float> dn = n * side;
+    if (c.voxel_offset_mode != FPT_VOXEL_OFFSET_PRECISION) return pos + dn * eps;
+    V3<float> r;
+    for (int a = 0; a < 3; ++a) {
+        const int off = int(256.0f * dn[a]);
+        int32_t bits = int32_t(float_bits(pos[a]));
+        bits += pos[a] < 0.0f ? -off : off;
+        r[a] = std::fabs(pos[a]) < 1.0f / 32.0f ? pos[a] + (1.0f / 65536.0f) * dn[a] : bits_float(uint32_t(bits));
+    }
+    return r;
+}
+
+// unpackVoxelMaterial (shaders/Shaders.metal:4023-4035).
+inline Material<float> voxel_material(const uint32_t *cell) {
+    Material<float> m;
+    const uint32_t pc = cell[0], pp = cell[1];
+    m.rgb = V3<float>(float(pc & 255u) / 255.0f, float((pc >> 8) & 255u) / 255.0f, float((pc >> 16) & 255u) / 255.0f);
+    m.roughness = float(pp & 255u) / 255.0f;
+    m.specular = float((pp >> 8) & 255u) / 255.0f;
+    m.translucency = float((pp >> 16) & 255u) / 255.0f;
+    m.ior = mixv(1.0f, 2.5f, float((pp >> 24) & 255u) / 255.0f);
+    m.emission = bits_float(cell[2]);
+    return m;
+}
+
+// renderVoxelPath (shaders/Shaders.metal:6526-6621) with face normals, stored
+// materials and no leaf refinement, and voxelSunContributionWithSurface
+// (6490-6515) for the sun term.
+inline V3<float> render_voxel_path(const VGrid &g, V2<float> uv, uint32_t pixel, uint32_t sample, float focus, const Cfg &c,
+                                   const Ext &e) {
+    PathRng rng{e.rng == FPT_CUDA_RNG_PCG, e.seed, pixel, sample, uv.x, uv.y, float(sample)};
+    V3<float> pos = cameraPos<float>(c);
+    const float focal = 1.0f / std::tan(c.camera_fov / 2.0f * float(kPi) / 180.0f);
+    const float aa = 0.3f / std::max(float(c.width), float(c.height));
+    const float h1 = rng.uniform(SLOT_LENS0, 0), h2 = rng.uniform(SLOT_LENS1, 0);
+    const V2<float> j = randomPoint(aa, h1, h2);
+    V3<float> dir = normalize(V3<float>(uv.x + j.x, uv.y + j.y, focal));
+    dir = rotateCamera(dir, c.camera_yaw_pitch[0], c.camera_yaw_pitch[1], c.camera_roll);
+    const V3<float> fp = pos + dir * focus;
+    const V2<float> lens = randomPoint(c.camera_dof, h1, h2);
+    pos = pos + rotateCamera(V3<float>(lens.x, lens.y, 0.0f), c.camera_yaw_pitch[0], c.camera_yaw_pitch[1], c.camera_roll);
+    dir = normalize(fp - pos);
+    V3<float> light(0.0f), color(1.0f);
+    float sky_mask = 0.0f;
+    const V3<float> grad = backgroundGradient(dir, c);
+    int bounces = std::min(int(c.render[0]), 8);
+    if (c.sdf_bounce_cap > 0u) bounces = std::min(bounces, int(c.sdf_bounce_cap));
+    const float cell = std::min(g.cs[0], std::min(g.cs[1], g.cs[2]));
+    const float eps = cell * 0.01f;
+    for (int b = 0; b < bounces; ++b) {
+        const VHit hit = trace(g, pos, dir, nullptr);
+        if (!hit.hit) {
+            if (b == 0) sky_mask = 1.0f;
+            light = light + environment(dir, c, e);
+            break;
+        }
+        const Material<float> mt = voxel_material(g.cells + size_t(hit.payload) * 3);
+        const V3<float> hp = pos + dir * hit.t;
+        if (mt.emission > 0.001f) light = light + mt.rgb * mt.emission;
+        V3<float> n = hit.normal;
+        if (dot(n, dir) > 0.0f) n = -n;
+        if (c.sun[0] == 1.0f) {
+            V3<float> ld = rotateCamera(V3<float>(0.0f, 0.0f, 1.0f), c.sun[1] * float(kPi) / 180.0f, c.sun[2] * float(kPi) / 180.0f);
+            const float a1 = rng.uniform(SLOT_SUN0, b), a2 = rng.uniform(SLOT_SUN1, b);
+            const float sa = std::sin(a1 * 2.0f * float(kPi)), ca = std::cos(a1 * 2.0f * float(kPi));
+            const float ss = std::sqrt(a2) * c.sun[4];
+            ld = rotateCamera(ld, ca * ss, sa * ss);
+            const VHit sh = trace(g, voxel_offset_origin(hp, n, ld, c, eps), ld, nullptr);
+            if (!sh.hit)
+                light = light + V3<float>(c.sun_color[0], c.sun_color[1], c.sun_color[2]) *
+                                    (c.sun[3] * std::max(dot(n, ld), 0.0f) * mt.roughness * (1.0f - mt.translucency));
+        }
+        const float rs = rng.uniform(SLOT_SCATTER, b), rf = rng.uniform(SLOT_FRESNEL, b);
+        bool transmitted = false;
+        const float f0 = std::pow((mt.ior - 1.0f) / (mt.ior + 1.0f), 2.0f);
+        const float ct = clampv(dot(n, -dir), 0.0f, 1.0f);
+        const float fres = f0 + (1.0f - f0) * pow5(1.0f - ct);
+        if (rs > mt.translucency) {
+            const V3<float> refl = vreflect(dir, n);
+            const V3<float> diffuse = randomVector(n, rng.uniform(SLOT_DIR0, b), rng.uniform(SLOT_DIR1, b));
+            dir = normalize(vmix(refl, diffuse, mt.roughness));
+            if (rf < fres * mt.specular) dir = refl;
+            else color = color * mt.rgb;
+        } else {
+            const V3<float> refr = vrefract(dir, n, 1.0f / mt.ior);
+            const V3<float> refl = vreflect(dir, n);
+            if (dot(refr, refr) < 0.000001f || !std::isfinite(refr.x) || rf < fres) {
+                dir = normalize(refl);
+            } else {
+                dir = normalize(refr);
+                color = color * (vmix(V3<float>(1.0f), mt.rgb, 0.35f) * (1.0f - fres * 0.5f));
+                transmitted = true;
+            }
+        }
+        pos = transmitted ? hp + dir * (cell * 1.05f) : voxel_offset_origin(hp, n, dir, c, eps);
+        if (c.sdf_russian_roulette != 0u && b + 1 < bounces && float(b + 1) >= c.sdf_rr_start) {
+            const float surv = clampv(maxc(color), clampv(c.sdf_rr_min_prob, 0.01f, 1.0f), 1.0f);
+            if (rng.uniform(SLOT_RR, b) > surv) break;
+            color = color / surv;
+        }
+    }
+    V3<float> col = light * color;
+    if (c.world[6] == 1.0f) col = vmix(col, grad, sky_mask);
+    return vmin(col, V3<float>(8.0f));
 }
 
 }  // namespace oracle
@@ -2146,6 +2289,134 @@ void oracle_voxel_primary(const FptRenderConfig *cfg, const FptCudaSceneExt *e, 
             }
         }
     }
+}
+
+// renderVoxelPath accumulated over all samples of each pixel of rows [y0, y1)
+// (voxel_accumulate_all_kernel, shaders/Shaders.metal:7977-7992) through a grid
+// of reference cells (brick_size 4: page table + bricks; 0: dense cells).
+// accum: W*H x 4 floats, row 0 at the bottom; the focus distance follows
+// estimateVoxelFocusDistance (:6517-6523) when the config gives none.
+void oracle_voxel_render(const FptRenderConfig *cfg, const FptCudaSceneExt *e, uint32_t brick_size, const uint32_t *table,
+                         const uint32_t *cells, uint32_t y0, uint32_t y1, float *accum) {
+    const FptRenderConfig &c = *cfg;
+    const Ext &ex = ext_or_default(e);
+    VGrid g;
+    for (int k = 0; k < 3; ++k) {
+        g.bmin[k] = c.voxel_bounds_min[k]; g.bmax[k] = c.voxel_bounds_max[k];
+        g.cs[k] = (c.voxel_bounds_max[k] - c.voxel_bounds_min[k]) / float(c.voxel_resolution);
+    }
+    g.res = c.voxel_resolution; g.bs = brick_size ? brick_size : 1; g.bg = brick_size ? (g.res + brick_size - 1) / brick_size : 0;
+    g.storage = brick_size == 0 ? 0u : 1u;
+    g.table = table; g.occ = nullptr; g.cells = cells;
+    float focus = c.focus_distance;
+    if (!(focus > 0.0f)) {
+        const float focal = 1.0f / std::tan(c.camera_fov / 2.0f * float(kPi) / 180.0f);
+        const V3<float> d = rotateCamera(normalize(V3<float>(0.0f, 0.0f, focal)), c.camera_yaw_pitch[0], c.camera_yaw_pitch[1],
+                                         c.camera_roll);
+        const VHit h = trace(g, cameraPos<float>(c), d, nullptr);
+        focus = h.hit && h.t > 0.001f ? h.t : 5.0f;
+    }
+    const uint32_t W = c.width, H = c.height, spp = std::min(std::max(c.samples, 1u), 512u);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long long yy = y0; yy < (long long)y1; ++yy) {
+        const uint32_t y = uint32_t(yy);
+        for (uint32_t x = 0; x < W; ++x) {
+            float u = (float(x) + 0.5f) / float(W) - 0.5f, v = (float(y) + 0.5f) / float(H) - 0.5f;
+            u = u * (float(W) / float(H));
+            V3<float> mean(0.0f);
+            for (uint32_t s = 0; s < spp; ++s)
+                mean = vmix(mean, render_voxel_path(g, V2<float>{u, v}, y * W + x, s, focus, c, ex), 1.0f / float(s + 1u));
+            float *o = accum + (size_t(y) * W + x) * 4;
+            o[0] = mean.x; o[1] = mean.y; o[2] = mean.z; o[3] = 1.0f;
+        }
+    }
+}
+
+// HDRI hydration of the reference (src/metal_bridge.mm:2163-2300): the
+// Radiance RLE reader (new-style scanlines, RGBE decode (m + 0.5) 2^(e - 136),
+// -Y / +X orientation flags), then the 32 x 16 box-filtered LUT with float
+// sums in raster order and the round-half-up float -> half conversion.
+// Returns 0 and fills lut (32*16*3 halves), or 1 with a message.
+static uint16_t reference_half(float value) {
+    const uint32_t bits = float_bits(value);
+    const uint32_t sign = (bits >> 16u) & 0x8000u;
+    int exponent = int((bits >> 23u) & 0xffu) - 127 + 15;
+    uint32_t mantissa = bits & 0x7fffffu;
+    if (exponent <= 0) {
+        if (exponent < -10) return uint16_t(sign);
+        mantissa = (mantissa | 0x800000u) >> uint32_t(1 - exponent);
+        return uint16_t(sign | ((mantissa + 0x1000u) >> 13u));
+    }
+    if (exponent >= 31) return uint16_t(sign | 0x7c00u);
+    return uint16_t(sign | (uint32_t(exponent) << 10u) | ((mantissa + 0x1000u) >> 13u));
+}
+
+int oracle_hdri_lut(const char *path, uint16_t *lut, char *error, size_t error_len) {
+    auto fail = [&](const std::string &m) { std::snprintf(error, error_len, "%s", m.c_str()); return 1; };
+    std::ifstream in(path, std::ios::binary);
+    if (!in) return fail(std::string("failed to open HDRI ") + path);
+    std::string line;
+    bool rle = false;
+    while (std::getline(in, line)) {
+        if (!line.empty() && line.back() == '\r') line.pop_back();
+        if (line.rfind("FORMAT=32-bit_rle_rgbe", 0) == 0) rle = true;
+        if (line.empty()) break;
+    }
+    if (!std::getline(in, line)) return fail("missing HDRI resolution");
+    char ys = 0, xs = 0;
+    int w = 0, h = 0;
+    if (std::sscanf(line.c_str(), " %cY %d %cX %d", &ys, &h, &xs, &w) != 4 || w <= 0 || h <= 0) return fail("bad resolution line");
+    if (!rle || w < 8 || w > 32767) return fail("unsupported non-RLE Radiance HDRI");
+    std::vector<float> rgb(size_t(w) * h * 3, 0.0f);
+    std::vector<uint8_t> scan(size_t(w) * 4);
+    for (int fy = 0; fy < h; ++fy) {
+        unsigned char hd[4];
+        in.read(reinterpret_cast<char *>(hd), 4);
+        if (!in || hd[0] != 2 || hd[1] != 2 || ((int(hd[2]) << 8) | hd[3]) != w) return fail("invalid HDRI scanline");
+        for (int ch = 0; ch < 4; ++ch) {
+            int x = 0;
+            while (x < w) {
+                unsigned char code = 0;
+                in.read(reinterpret_cast<char *>(&code), 1);
+                if (!in || code == 0) return fail("truncated HDRI scanline");
+                if (code > 128) {
+                    unsigned char v = 0;
+                    in.read(reinterpret_cast<char *>(&v), 1);
+                    const int n = code - 128;
+                    if (!in || x + n > w) return fail("corrupt HDRI run");
+                    for (int k = 0; k < n; ++k) scan[size_t(x++) * 4 + ch] = v;
+                } else {
+                    if (x + code > w) return fail("corrupt HDRI literal");
+                    for (int k = 0; k < code; ++k) {
+                        unsigned char v = 0;
+                        in.read(reinterpret_cast<char *>(&v), 1);
+                        scan[size_t(x++) * 4 + ch] = v;
+                    }
+                }
+            }
+        }
+        const int oy = ys == '-' ? fy : h - 1 - fy;
+        for (int fx = 0; fx < w; ++fx) {
+            const int ox = xs == '+' ? fx : w - 1 - fx;
+            const uint8_t e = scan[size_t(fx) * 4 + 3];
+            const float sc = e == 0 ? 0.0f : std::ldexp(1.0f, int(e) - 136);
+            for (int k = 0; k < 3; ++k) rgb[(size_t(oy) * w + ox) * 3 + k] = (float(scan[size_t(fx) * 4 + k]) + 0.5f) * sc;
+        }
+    }
+    const uint32_t LW = FPT_HDRI_LUT_WIDTH, LH = FPT_HDRI_LUT_HEIGHT, W = uint32_t(w), H = uint32_t(h);
+    for (uint32_t y = 0; y < LH; ++y) {
+        const uint32_t sy0 = uint32_t(uint64_t(y) * H / LH), sy1 = std::max(sy0 + 1u, uint32_t(uint64_t(y + 1) * H / LH));
+        for (uint32_t x = 0; x < LW; ++x) {
+            const uint32_t sx0 = uint32_t(uint64_t(x) * W / LW), sx1 = std::max(sx0 + 1u, uint32_t(uint64_t(x + 1) * W / LW));
+            float sum[3] = {0.0f, 0.0f, 0.0f};
+            uint32_t n = 0;
+            for (uint32_t sy = sy0; sy < std::min(sy1, H); ++sy)
+                for (uint32_t sx = sx0; sx < std::min(sx1, W); ++sx, ++n)
+                    for (int k = 0; k < 3; ++k) sum[k] += rgb[(size_t(sy) * W + sx) * 3 + k];
+            for (int k = 0; k < 3; ++k) lut[(size_t(y) * LW + x) * 3 + k] = reference_half(sum[k] / float(std::max(n, 1u)));
+        }
+    }
+    return 0;
 }
 
 // voxel_dda_contract_test cases (shaders/Shaders.metal:5164-5211); bit k = failed case k.

@@ -3,8 +3,10 @@
 The reference (Rust + Metal) cannot be built here, so these vectors are the
 expected values its tests assert, restated as data:
   * orbit_known_answers.json -- src/mandelbulber/orbit.rs:1866-1960
-    (classic Mandelbulb power 2, full Mandelbox with scale -1.5), with the
-    closed forms the Rust tests use (2*sqrt(14)+1, |z| = 14, (-0.6, -1.2, -1.8), dr = 7).
+    (quadratic triplex "mandelbulb power 2", classic Mandelbulb power 2, full
+    Mandelbox with scale -1.5), with the closed forms the Rust tests use
+    ((2.4, -3.2, -6*sqrt(5)) and dr = 2*sqrt(14); 2*sqrt(14)+1 and |z| = 14;
+    (-0.6, -1.2, -1.8), dr = 7 and colour 1.2).
   * dda_contract.json -- the voxel cell-ownership / DDA / AABB cases of
     voxel_dda_contract_test, shaders/Shaders.metal:5164-5211.
 Run:  python tests/golden/make_golden.py
@@ -25,11 +27,14 @@ def main():
     orbit = {
         "source": "src/mandelbulber/orbit.rs:1866-1960",
         "cases": [
+            {"name": "mandelbulb_power2_triplex", "formula": "mandelbulb_power2", "point": [1.0, 2.0, 3.0, 0.0],
+             "expect": {"z": [2.4, -3.2, -6.0 * math.sqrt(5.0), 0.0], "derivative": 2.0 * math.sqrt(14.0)},
+             "tolerance": 1e-12, "source": "src/mandelbulber/orbit.rs:1866-1874"},
             {"name": "classic_mandelbulb_power2", "formula": "mandelbulb", "power": 2.0, "point": [1.0, 2.0, 3.0, 0.0],
              "expect": {"derivative": 2.0 * math.sqrt(14.0) + 1.0, "length": 14.0}, "tolerance": 1e-12},
             {"name": "full_mandelbox_unrotated", "formula": "mandelbox", "scale": -1.5, "folding_limit": 1.0,
              "folding_value": 2.0, "fixed_radius": 1.0, "minimum_radius": 0.5, "point": [0.1, 0.2, 0.3, 0.0],
-             "expect": {"z": [-0.6, -1.2, -1.8, 0.0], "derivative": 7.0}, "tolerance": 1e-12},
+             "expect": {"z": [-0.6, -1.2, -1.8, 0.0], "derivative": 7.0, "color": 1.2}, "tolerance": 1e-12},
         ],
     }
     with open(os.path.join(HERE, "orbit_known_answers.json"), "w") as f:

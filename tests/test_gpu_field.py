@@ -89,3 +89,21 @@ def test_batch_scene_fields(native, k):
           np.percentile(np.abs(g[:, 0] - r[:, 0]) / (1 + np.abs(r[:, 0])), 99))
     _gate(g[:, 0], r[:, 0], outliers=5e-3)
     assert np.mean(g[:, 3] == r[:, 3]) > 0.99   # iteration counts
+
+
+def test_mandelbulb_power2_triplex_field(native):
+    """Mandelbulber formula 3, the quadratic triplex of orbit.rs:752-764 (known answer pinned on the CPU at
+    orbit.rs:1866-1874), marched as a scene: GPU field and analytic gradient against the FP64 oracle."""
+    cfg, ext = scenes.mandelbulb_primary(8, 8)
+    ext.formula = ffi.FORMULA_MANDELBULB_POWER2
+    ext.iterations = 10
+    ext.bailout = 4.0
+    p = pts(1 << 16, -1.6, 1.6, seed=5)
+    g, gg = native.sample_distance(cfg, ext, p, gradients=True)
+    r, gr = oracle.sample_distance(cfg, ext, p, fp64=True, gradients=True)
+    _gate(g[:, 0], r[:, 0])
+    assert np.mean(g[:, 3] == r[:, 3]) > 0.999
+    ng, nr = np.linalg.norm(gg, axis=1), np.linalg.norm(gr, axis=1)
+    ok = (nr > 1e-6) & np.isfinite(ng) & (np.abs(r[:, 0]) > 1e-3)
+    cosang = (gg[ok] * gr[ok]).sum(1) / (ng[ok] * nr[ok])
+    assert np.percentile(np.degrees(np.arccos(np.clip(cosang, -1, 1))), 99) < 0.5

@@ -20,6 +20,8 @@ def _orbit_ext(case):
     if case["formula"] == "mandelbulb":
         e.formula = ffi.FORMULA_MANDELBULB
         e.power = case["power"]
+    elif case["formula"] == "mandelbulb_power2":
+        e.formula = ffi.FORMULA_MANDELBULB_POWER2
     else:
         e.formula = ffi.FORMULA_MANDELBOX
         e.box_scale = case["scale"]
@@ -42,6 +44,8 @@ def test_orbit_known_answers(oracle_lib):
             assert abs(math.sqrt((z ** 2).sum()) - exp["length"]) < tol, case["name"]
         if "z" in exp:
             assert np.allclose(z, exp["z"], atol=tol, rtol=0), case["name"]
+        if "color" in exp:
+            assert abs(out[9] - exp["color"]) < tol, case["name"]
 
 
 def test_logarithmic_finalizer_edges(oracle_lib):
