@@ -447,6 +447,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     pl.scene = c.scene; pl.kind = S.kind; pl.width = S.width; pl.height = S.height; pl.bounces = S.bounces;
     pl.accum = c.accum; pl.counters = c.counter; pl.march_blocks = c.march_blocks;
     pl.refill_batch = c.refill_batch;
+    pl.fp64 = (S.fp64_bisection && S.sdf_id == FPT_SDF_MANDELBULBER && S.formula != 0 && !(S.camera_dof > 0.0f)) ? 1u : 0u;
     pl.loop_limit_ns = c.loop_limit_ns;
     pl.profile = want_profile ? c.profile : nullptr;
     {
@@ -458,6 +459,10 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         pl.wave_paths = uint32_t(cap);
         if (!ensure_buffer(&c.wave, &c.cap_wave, wave_scratch_bytes(cap), error, error_len)) return 1;
         pl.wave_scratch = c.wave;
+        if (want_profile) {
+            if (!ensure_buffer((void **)&c.path_steps, &c.cap_path_steps, cap * sizeof(uint32_t), error, error_len)) return 1;
+            pl.path_steps = c.path_steps;
+        }
     }
     pl.sample_rgb = c.sample_rgb;
     SkipArgs skip;
@@ -559,6 +564,10 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
         profile_out->refinement_steps = v[11];
         profile_out->refinement_distance_evals = v[11];
         profile_out->max_ray_steps = v[12];
+        profile_out->max_pixel_steps = v[13];
+        profile_out->orbit_iterations_by_phase[3] = v[14];
+        profile_out->march_orbit_iterations += v[14];
+        profile_out->formula_slot_iterations[0] = profile_out->march_orbit_iterations;
         // Render time apportioned by counted work units (src/metal_bridge.mm:5712-5733).
         const double units[5] = {double(v[0]), double(v[1]), double(v[2]), double(profile_out->normal_field_evals), double(v[4])};
         const double total = units[0] + units[1] + units[2] + units[3] + units[4];

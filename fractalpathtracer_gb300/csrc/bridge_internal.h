@@ -24,6 +24,7 @@ struct Context {
     uchar4 *rgba = nullptr; size_t cap_rgba = 0;
     unsigned int *counter = nullptr; size_t cap_counter = 0;
     unsigned long long *profile = nullptr; size_t cap_profile = 0;
+    uint32_t *path_steps = nullptr; size_t cap_path_steps = 0;   // profile renders: march steps per path of a wave
     float *sky = nullptr; size_t cap_sky = 0;
     FptCudaPrimaryHit *hits = nullptr; size_t cap_hits = 0;
     float4 *points = nullptr; size_t cap_points = 0;

@@ -944,7 +944,7 @@ static __device__ Material material_of(const DeviceScene &S, const Eval &e) {
 // Analytic gradient of the extension distance (dual numbers), or the typed
 // program's Jacobian gradient.  Returns false when no analytic form applies.
 template <int KIND>
-static __device__ bool analytic_gradient(const DeviceScene &S, float3 p, float3 &g) {
+static __device__ bool analytic_gradient(const DeviceScene &S, float3 p, float3 &g, uint32_t *orbit_iters = nullptr) {
     if (S.formula != 0) {
         D4 x(p.x, 1.f, 0.f, 0.f), y(p.y, 0.f, 1.f, 0.f), z(p.z, 0.f, 0.f, 1.f);
         OrbitResult<D4> o;
@@ -958,6 +958,7 @@ static __device__ bool analytic_gradient(const DeviceScene &S, float3 p, float3 
         }
         g = mk3(o.d.x, o.d.y, o.d.z);
         if (S.ground_plane && p.y - S.plane_height < o.d.v) g = mk3(0.f, 1.f, 0.f);
+        if (orbit_iters) *orbit_iters += uint32_t(o.iterations);
         return true;
     }
     if (S.sdf_id == FPT_SDF_PROGRAM && S.program_count > 0u && (S.normal_mode == 0u || S.normal_mode == 2u)) {

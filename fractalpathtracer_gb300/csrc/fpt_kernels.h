@@ -50,13 +50,15 @@ struct PathLaunch {
     unsigned int *counters;     // 8 device words
     uint32_t sample_begin, sample_end;
     int march_blocks;           // persistent march grid, <= 0 = one wave of resident blocks
-    unsigned long long *profile;  // 8 device counters or null
+    unsigned long long *profile;  // kProfileSlots device counters or null
+    uint32_t *path_steps;       // profile renders: wave_paths words (march steps per path), or null
     const SkipArgs *skip;       // surrogate-skip pass before each march pass, or null
     KernelTimer *timer;         // per-kernel event spans, or null
     uint64_t *launches;         // host counter of kernel launches, or null
     uint32_t *grids;            // out: blocks of the persistent march and skip grids (2 entries), or null
     unsigned long long loop_limit_ns;   // time limit of the persistent loops (0: 10 s)
     uint32_t refill_batch;      // lockstep: finished lanes finish and refill together in groups of this many
+    uint32_t fp64;              // camera-ray pass continues stalled FP32 marches in FP64 (deep zoom, pinhole camera)
 };
 
 cudaError_t launch_pathtrace(const PathLaunch &pl, cudaStream_t stream);

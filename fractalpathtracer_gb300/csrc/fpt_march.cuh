@@ -215,6 +215,26 @@ __device__ bool march_fp64(const DeviceScene &S, float3 origin, float3 dir, doub
     return true;
 }
 
+// Normal at an FP64 hit point: central differences of |DE| in FP64 with the
+// normal epsilon of normalAt (the Mandelbulber threshold at the point times
+// vset_values[114], shaders/Shaders.metal:3899-3901).  At deep zoom the FP32
+// hit position is many thresholds from the surface, so a normal evaluated
+// there would belong to other detail.
+template <int KIND>
+__device__ __noinline__ float3 normal_fp64(const DeviceScene &S, double px, double py, double pz) {
+    const float *v = S.vset_values;
+    const double ex = px - double(S.cam_pos[0]), ey = py - double(S.cam_pos[1]), ez = pz - double(S.cam_pos[2]);
+    double th = v[115] > 0.5f ? sqrt(ex * ex + ey * ey + ez * ez) * double(v[116]) : double(v[117]);
+    th = fmin(fmax(th, double(v[118])), double(v[119]));
+    const double e = th * double(v[114]);
+    const double gx = fabs(de_fp64<KIND>(S, px + e, py, pz)) - fabs(de_fp64<KIND>(S, px - e, py, pz));
+    const double gy = fabs(de_fp64<KIND>(S, px, py + e, pz)) - fabs(de_fp64<KIND>(S, px, py - e, pz));
+    const double gz = fabs(de_fp64<KIND>(S, px, py, pz + e)) - fabs(de_fp64<KIND>(S, px, py, pz - e));
+    const double n = sqrt(gx * gx + gy * gy + gz * gz);
+    if (!(n > 0.0) || !isfinite(n)) return mk3(0.0f, 1.0f, 0.0f);
+    return mk3(float(gx / n), float(gy / n), float(gz / n));
+}
+
 // Plain-loop march (focus prepass, primary rays, diagnostics).
 template <int KIND>
 __device__ March march_loop(const DeviceScene &S, float3 origin, float3 dir, int ni, float min_dist, float lod_falloff) {
@@ -307,13 +327,15 @@ __device__ __forceinline__ bool normal_is_analytic(const DeviceScene &S) {
 }
 
 // normalAt in straight-line form (shaders/Shaders.metal:3871-3971).
-template <int KIND> __device__ float3 normal_direct(float3 p, const DeviceScene &S) {
+// orbit_iters (optional) gets the orbit iterations of the analytic or tap
+// evaluations (the normal phase of FptSdfProfileStats).
+template <int KIND> __device__ float3 normal_direct(float3 p, const DeviceScene &S, uint32_t *orbit_iters = nullptr) {
     if (S.sdf_id == FPT_SDF_MANDELBULBER && S.render[7] > 0.0f && !(S.formula != 0 && S.ext_normal == FPT_CUDA_NORMAL_ANALYTIC))
         return mandel_slow_normal<KIND>(p, S);
     float3 g;
     if ((S.formula != 0 && S.ext_normal == FPT_CUDA_NORMAL_ANALYTIC) ||
         (S.formula == 0 && S.sdf_id == FPT_SDF_PROGRAM)) {
-        if (analytic_gradient<KIND>(S, p, g)) {
+        if (analytic_gradient<KIND>(S, p, g, orbit_iters)) {
             if (S.formula != 0) {
                 if (finite3(g) && dot(g, g) > 0.0f) return normalize3(g);
                 return mk3(0.f, 1.f, 0.f);
@@ -324,7 +346,11 @@ template <int KIND> __device__ float3 normal_direct(float3 p, const DeviceScene 
     float e = normal_epsilon(p, S);
     float3 acc = mk3(0.0f);
     int n = tap_count(S), mode = tap_mode(S);
-    for (int k = 0; k < n; ++k) tap_accumulate(S, k, scene_eval<KIND>(S, p + tap_offset(S, k, e), mode).d, acc);
+    for (int k = 0; k < n; ++k) {
+        const Eval ev = scene_eval<KIND>(S, p + tap_offset(S, k, e), mode);
+        if (orbit_iters) *orbit_iters += uint32_t(ev.iters);
+        tap_accumulate(S, k, ev.d, acc);
+    }
     if (S.normal_mode != 1u && S.sdf_id == FPT_SDF_MANDELBULBER && !(fmaxf(fabsf(acc.x), fmaxf(fabsf(acc.y), fabsf(acc.z))) > 0.0f))
         acc = mandel_orbit_normal<KIND>(p, e, S);
     return normalize_fd(acc);

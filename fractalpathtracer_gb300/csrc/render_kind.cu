@@ -40,6 +40,7 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
     W.sample_rgb = pl.sample_rgb;
     W.counters = pl.counters;
     W.profile = pl.profile;
+    W.path_steps = pl.profile ? pl.path_steps : nullptr;
     W.box_on = pl.skip ? 1u : 0u;
     for (int k = 0; k < 3; ++k) {
         W.box_lo[k] = pl.skip ? pl.skip->lo[k] : 0.0f;
@@ -66,6 +67,15 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<KIND>, 128, 0);
         march_blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
+    // Deep zoom: the camera-ray pass runs the march variant with the FP64 continuation (extension formulas).
+    constexpr bool kExt = KIND == KIND_BULB8 || KIND == KIND_BULB || KIND == KIND_BOX || KIND == KIND_MENGER || KIND == KIND_HYBRID;
+    const bool fp64 = kExt && pl.fp64 && !pl.skip;
+    int fp64_blocks = march_blocks;
+    if (fp64 && pl.march_blocks <= 0) {
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, march_kernel<KIND, false, 128, 7, kExt>, 128, 0);
+        fp64_blocks = sms * (per > 0 ? per : 1);
+    }
     const bool skip_tc = skip_pass && pl.skip->engine == kNetTcgen05;
     const int skip_blocks = skip_pass ? FPT_CAT(skip_pass_blocks_k, FPT_KIND)(skip_tc, sms) : 0;
     if (pl.grids) {
@@ -88,6 +98,8 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         W.wave_base = uint32_t(wb);
         W.n_paths = uint32_t(std::min<uint64_t>(cap, total - wb));
         if ((e = cudaMemsetAsync(W.counters, 0, C_COUNT * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+        if (W.path_steps && (e = cudaMemsetAsync(W.path_steps, 0, size_t(W.n_paths) * sizeof(uint32_t), stream)) != cudaSuccess)
+            return e;
         if (W.box_on && wb == 0) {
             first_step_kernel<KIND><<<1, 32, 0, stream>>>(pl.scene, W.counters + C_CAMSTEP);
             ++launches;
@@ -103,7 +115,10 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
             // the camera rays only, the box clip applies in every pass.
             if (skip_pass && b == 0u)
                 timed(KC_SKIP, [&] { FPT_CAT(launch_skip_pass_k, FPT_KIND)(W, *pl.skip, skip_tc, skip_blocks, stream); });
-            timed(KC_MARCH, [&] { march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur); });
+            timed(KC_MARCH, [&] {
+                if (fp64 && b == 0u) march_kernel<KIND, false, 128, 7, kExt><<<fp64_blocks, 128, 0, stream>>>(W, cur);
+                else march_kernel<KIND><<<march_blocks, 128, 0, stream>>>(W, cur);
+            });
             if (b < pl.bounces) timed(KC_SHADE, [&] { shade_kernel<KIND><<<shade_blocks, 128, 0, stream>>>(W, cur); });
         }
         finalize_kernel<false><<<(W.n_paths + 255u) / 256u, 256, 0, stream>>>(W);

@@ -5,17 +5,23 @@
 // source order, so brick tables and cell sequences are bit-identical to the
 // CPU restatement for estimators made of IEEE operations (+ - * / sqrt).
 //
-// Build pipeline (one resident grid per process):
-//   brick_classify_kernel  one CTA per brick, one thread per cell: distance at
-//                          the cell centre, occupancy (classifyAccelerationCell,
+// Build pipeline of occupancy bricks (one resident grid per process):
+//   brick_stage_kernel     one CTA per 8^3 brick, one thread per cell: distance
+//                          at the cell centre and occupancy (classifyAccelerationCell,
 //                          shaders/Shaders.metal:4196-4244, legacy coverage),
-//                          per-brick occupied-cell count
+//                          each evaluated once; the brick is assembled in shared
+//                          memory (512 occupancy bytes, 512 fp16 distances, the
+//                          64-byte bit mask) and an occupied brick leaves as 100
+//                          16-byte vector stores into a staging slot of its own
 //   scan kernels           exclusive scan of "brick occupied" in raster order
 //                          (brick x fastest): the compaction order of the
 //                          reference's host finalize_voxel_storage
 //                          (src/metal_bridge.mm:1738-1812), deterministic
-//   brick_fill_kernel      occupied bricks only: recompute the cells, write the
-//                          payload into the brick's compact slot
+//   brick_commit_kernel    one warp per brick: the brick table entry, and for an
+//                          occupied brick a 16-byte-vector copy of its staged
+//                          payload into its compact slot
+// Reference cells (4^3 bricks) keep two passes: brick_classify_kernel counts,
+// brick_fill_kernel evaluates the occupied bricks' cells and materials.
 // Formats: reference (4^3 bricks of 12-byte VoxelCell, shaders/Shaders.metal:
 // 3973-4044) and occupancy bricks (8^3 bricks, uint8 occupancy + fp16
 // distance per cell, plus a 64-byte occupancy bitmask per brick for the DDA).
@@ -137,6 +143,66 @@ __global__ void __launch_bounds__(256) scan_add_kernel(uint32_t *offset, uint32_
     if (i < n) offset[i] += block_sums[i / kScanBlock];
 }
 
+// Occupancy bricks, classified once: a brick's 100 16-byte vectors (32 of
+// occupancy bytes, 64 of fp16 distances, 4 of bit mask) in its staging slot.
+constexpr uint32_t kBrickVectors = 100;
+constexpr size_t kBrickStageBytes = size_t(kBrickVectors) * 16;
+template <int KIND>
+__global__ void __launch_bounds__(512) brick_stage_kernel(const DeviceScene *scene, VoxBuild B, uint32_t *brick_count,
+                                                          unsigned long long *active_cells, uint4 *stage) {
+    __shared__ __align__(16) uint8_t s_occ[512];
+    __shared__ __align__(16) __half s_dist[512];
+    __shared__ __align__(16) uint32_t s_mask[16];
+    const DeviceScene &S = *scene;
+    const uint32_t b = blockIdx.x;
+    const uint32_t bx = b % B.brick_grid, by = (b / B.brick_grid) % B.brick_grid, bz = b / (B.brick_grid * B.brick_grid);
+    const uint32_t l = threadIdx.x;
+    const uint32_t x = bx * 8u + (l & 7u), y = by * 8u + ((l >> 3) & 7u), z = bz * 8u + (l >> 6);
+    bool occ = false;
+    float d = 0.0f;
+    const bool inside = x < B.res && y < B.res && z < B.res;
+    if (inside) {
+        float3 p;
+        occ = classify_cell<KIND>(S, B, x, y, z, d, p);
+    }
+    s_occ[l] = occ ? 1u : 0u;
+    s_dist[l] = __float2half_rn(inside ? d : 0.0f);
+    const unsigned bal = __ballot_sync(0xffffffffu, occ);
+    if ((l & 31u) == 0u) s_mask[l >> 5] = bal;
+    const int count = __syncthreads_count(occ);   // also orders the shared-memory writes before the copy-out
+    if (count > 0) {
+        uint4 *dst = stage + size_t(b) * kBrickVectors;
+        if (l < 32u) dst[l] = reinterpret_cast<const uint4 *>(s_occ)[l];
+        else if (l < 96u) dst[l] = reinterpret_cast<const uint4 *>(s_dist)[l - 32u];
+        else if (l < kBrickVectors) dst[l] = reinterpret_cast<const uint4 *>(s_mask)[l - 96u];
+    }
+    if (l == 0u) {
+        brick_count[b] = uint32_t(count);
+        if (count) atomicAdd(active_cells, (unsigned long long)count);
+    }
+}
+__global__ void __launch_bounds__(256) brick_commit_kernel(const uint32_t *brick_count, const uint32_t *brick_offset, uint32_t nb,
+                                                           const uint4 *stage, uint32_t *table, uint4 *occ_out, uint4 *dist_out,
+                                                           uint4 *mask_out) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nb; b += warps) {
+        if (brick_count[b] == 0u) {
+            if (lane == 0u) table[b] = 0u;
+            continue;
+        }
+        const uint32_t id = brick_offset[b];
+        if (lane == 0u) table[b] = id + 1u;
+        const uint4 *src = stage + size_t(b) * kBrickVectors;
+        for (uint32_t k = lane; k < kBrickVectors; k += 32u) {
+            const uint4 v = src[k];
+            if (k < 32u) occ_out[size_t(id) * 32u + k] = v;
+            else if (k < 96u) dist_out[size_t(id) * 64u + (k - 32u)] = v;
+            else mask_out[size_t(id) * 4u + (k - 96u)] = v;
+        }
+    }
+}
+
 // Packs a unorm4 the way packVoxelUnorm4 does (shaders/Shaders.metal:4018-4021).
 __device__ __forceinline__ uint32_t pack_unorm4(float a, float b, float c, float d) {
     uint32_t q0 = uint32_t(rintf(fminf(fmaxf(a, 0.f), 1.f) * 255.0f)), q1 = uint32_t(rintf(fminf(fmaxf(b, 0.f), 1.f) * 255.0f));
@@ -144,10 +210,12 @@ __device__ __forceinline__ uint32_t pack_unorm4(float a, float b, float c, float
     return q0 | (q1 << 8) | (q2 << 16) | (q3 << 24);
 }
 
-template <int KIND, int BS, int FMT>
+// Reference cells: occupied bricks only, each cell re-evaluated with its
+// material (buildVoxelCell, shaders/Shaders.metal:5388-5414) into the brick's
+// compact slot.
+template <int KIND, int BS>
 __global__ void __launch_bounds__(BS *BS *BS) brick_fill_kernel(const DeviceScene *scene, VoxBuild B, const uint32_t *brick_count,
-                                                                const uint32_t *brick_offset, uint32_t *table, uint8_t *occ_out,
-                                                                __half *dist_out, uint32_t *mask_out, uint32_t *cells_out) {
+                                                                const uint32_t *brick_offset, uint32_t *table, uint32_t *cells_out) {
     const DeviceScene &S = *scene;
     uint32_t b = blockIdx.x;
     if (brick_count[b] == 0u) {
@@ -165,24 +233,16 @@ __global__ void __launch_bounds__(BS *BS *BS) brick_fill_kernel(const DeviceScen
     bool inside = x < B.res && y < B.res && z < B.res;
     if (inside) occ = classify_cell<KIND>(S, B, x, y, z, d, p);
     size_t slot = size_t(id) * (BS * BS * BS) + l;
-    if (FMT == VF_OCCUPANCY) {
-        occ_out[slot] = occ ? 1u : 0u;
-        dist_out[slot] = __float2half_rn(inside ? d : 0.0f);
-        unsigned bal = __ballot_sync(0xffffffffu, occ);
-        if ((l & 31u) == 0u) mask_out[slot >> 5] = bal;
-    } else {
-        // buildVoxelCell (shaders/Shaders.metal:5388-5414)
-        uint32_t c0 = 0u, c1 = 0u, c2 = 0u;
-        if (occ) {
-            Material m = material_of(S, scene_eval<KIND>(S, p, EV_MATERIAL));
-            c0 = pack_unorm4(m.rgb.x, m.rgb.y, m.rgb.z, 0.0f) | 0x80000000u;
-            c1 = pack_unorm4(m.roughness, m.specular, m.translucency, (m.ior - 1.0f) / 1.5f);
-            c2 = __float_as_uint(m.emission);
-        }
-        cells_out[slot * 3 + 0] = c0;
-        cells_out[slot * 3 + 1] = c1;
-        cells_out[slot * 3 + 2] = c2;
+    uint32_t c0 = 0u, c1 = 0u, c2 = 0u;
+    if (occ) {
+        Material m = material_of(S, scene_eval<KIND>(S, p, EV_MATERIAL));
+        c0 = pack_unorm4(m.rgb.x, m.rgb.y, m.rgb.z, 0.0f) | 0x80000000u;
+        c1 = pack_unorm4(m.roughness, m.specular, m.translucency, (m.ior - 1.0f) / 1.5f);
+        c2 = __float_as_uint(m.emission);
     }
+    cells_out[slot * 3 + 0] = c0;
+    cells_out[slot * 3 + 1] = c1;
+    cells_out[slot * 3 + 2] = c2;
 }
 
 // Dense reference storage: every cell (voxel_build_kernel, shaders/Shaders.metal:5416-5424).
@@ -267,7 +327,7 @@ __global__ void __launch_bounds__(128) voxel_primary_kernel(vox::Grid g, CamExac
     float2 uv = exact_uv(gx, gy, W, H);
     float3 d = exact_camera_dir(C, uv.x, uv.y);
     float3 o = make_float3(C.pos[0], C.pos[1], C.pos[2]);
-    vox::Hit h = vox::trace(g, o, d, nullptr, 0, nullptr, nullptr);
+    vox::Hit h = vox::trace_bricks(g, o, d);
     FptCudaVoxelHit out;
     out.t = h.hit ? h.t : -1.0f;
     out.cell = h.hit ? uint32_t(h.cell.x) + uint32_t(h.cell.y) * g.res + uint32_t(h.cell.z) * g.res * g.res : 0xffffffffu;
@@ -283,7 +343,7 @@ __global__ void __launch_bounds__(128) voxel_primary_kernel(vox::Grid g, CamExac
         float3 n = h.normal;
         if (n.x * d.x + n.y * d.y + n.z * d.z > 0.0f) n = make_float3(-n.x, -n.y, -n.z);
         float3 so = offset_origin(pos, n, sun, eps);
-        vox::Hit s = vox::trace(g, so, sun, nullptr, 0, nullptr, nullptr);
+        vox::Hit s = vox::trace_bricks(g, so, sun);
         out.shadow_steps = s.steps ? s.steps : 0u;
         out.lit = s.hit ? 0u : 1u;
         float ndl = fmaxf(n.x * sun.x + n.y * sun.y + n.z * sun.z, 0.0f);
@@ -484,6 +544,7 @@ struct VoxelState {
     uint8_t *occ = nullptr; size_t cap_occ = 0;
     __half *dist = nullptr; size_t cap_dist = 0;
     uint32_t *mask = nullptr; size_t cap_mask = 0;
+    uint4 *stage = nullptr; size_t cap_stage = 0;   // occupancy bricks: one staging slot per brick
     uint32_t *cells = nullptr; size_t cap_cells = 0;
     float *rays = nullptr; size_t cap_rays = 0;
     uint32_t *seq = nullptr; size_t cap_seq = 0;
@@ -515,8 +576,14 @@ static bool launch_build(const DeviceScene *scene, const VoxBuild &B, uint32_t b
                          size_t error_len) {
     VoxelState &V = vstate();
     const uint32_t nb = B.brick_grid * B.brick_grid * B.brick_grid;
-    if (bs == 8) brick_classify_kernel<KIND, 8><<<nb, 512, 0, st>>>(scene, B, V.count, V.stats);
-    else brick_classify_kernel<KIND, 4><<<nb, 64, 0, st>>>(scene, B, V.count, V.stats);
+    if (format == VF_OCCUPANCY) {
+        if (!ensure_buffer((void **)&V.stage, &V.cap_stage, size_t(nb) * kBrickStageBytes, error, error_len)) return false;
+        brick_stage_kernel<KIND><<<nb, 512, 0, st>>>(scene, B, V.count, V.stats, V.stage);
+    } else if (bs == 8) {
+        brick_classify_kernel<KIND, 8><<<nb, 512, 0, st>>>(scene, B, V.count, V.stats);
+    } else {
+        brick_classify_kernel<KIND, 4><<<nb, 64, 0, st>>>(scene, B, V.count, V.stats);
+    }
     uint32_t nblocks = (nb + kScanBlock - 1) / kScanBlock;
     scan_blocks_kernel<<<nblocks, kScanThreads, 0, st>>>(V.count, nb, V.offset, V.sums);
     scan_sums_kernel<<<1, kScanThreads, 0, st>>>(V.sums, nblocks, reinterpret_cast<uint32_t *>(V.stats + 1));
@@ -535,13 +602,15 @@ static bool launch_build(const DeviceScene *scene, const VoxBuild &B, uint32_t b
         if (!ensure_buffer((void **)&V.occ, &V.cap_occ, cells, error, error_len)) return false;
         if (!ensure_buffer((void **)&V.dist, &V.cap_dist, cells * sizeof(__half), error, error_len)) return false;
         if (!ensure_buffer((void **)&V.mask, &V.cap_mask, (cells + 31) / 32 * 4, error, error_len)) return false;
-        brick_fill_kernel<KIND, 8, VF_OCCUPANCY><<<nb, 512, 0, st>>>(scene, B, V.count, V.offset, V.table, V.occ, V.dist, V.mask,
-                                                                     nullptr);
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx().device);
+        const uint32_t blocks = std::min<uint32_t>((nb + 7u) / 8u, uint32_t(std::max(sms, 1)) * 32u);
+        brick_commit_kernel<<<blocks, 256, 0, st>>>(V.count, V.offset, nb, V.stage, V.table, reinterpret_cast<uint4 *>(V.occ),
+                                                     reinterpret_cast<uint4 *>(V.dist), reinterpret_cast<uint4 *>(V.mask));
         V.memory_bytes = size_t(nb) * 4 + cells * (1 + 2) + (cells + 31) / 32 * 4;
     } else {
         if (!ensure_buffer((void **)&V.cells, &V.cap_cells, cells * 12, error, error_len)) return false;
-        brick_fill_kernel<KIND, 4, VF_REFERENCE><<<nb, 64, 0, st>>>(scene, B, V.count, V.offset, V.table, nullptr, nullptr, nullptr,
-                                                                     V.cells);
+        brick_fill_kernel<KIND, 4><<<nb, 64, 0, st>>>(scene, B, V.count, V.offset, V.table, V.cells);
         V.memory_bytes = size_t(nb) * 4 + cells * 12;
     }
     return check(cudaGetLastError(), "voxel fill launch", error, error_len);

@@ -201,5 +201,88 @@ __device__ __forceinline__ Hit trace(const Grid &g, float3 o, float3 d, uint32_t
     return h;
 }
 
+// trace() specialised for occupancy bricks (8^3 cells, bit mask per brick)
+// and for the render: one loop iteration per visited cell for every lane, so
+// a warp's lanes stay in step (per-lane brick caching and per-lane inner
+// loops over empty bricks were measured slower: whichever lane enters a new
+// brick or leaves an empty one makes the whole warp run that code on most
+// trips).  Per cell: the brick-table word (shift arithmetic, read-only
+// cache), for an occupied brick one mask word, and the advance without the
+// entry-normal writes -- the face normal is rebuilt at the hit from the axis
+// crossed last.  Cells, entry distance, normal and step count equal trace()'s.
+__device__ __forceinline__ Hit trace_bricks(const Grid &g, float3 o, float3 d) {
+    Hit h;
+    h.hit = false; h.t = kInfF; h.exit_t = kInfF; h.cell = make_int3(0, 0, 0); h.normal = make_float3(0.f, 0.f, 0.f);
+    h.steps = 0; h.brick_fetches = 0;
+    float near_t, far_t;
+    float3 en;
+    if (!ray_aabb(o, d, g.bmin, g.bmax, near_t, far_t, en)) return h;
+    float entry_t = fmaxf(near_t, 0.0f);
+    float3 start = make_float3(fminf(fmaxf(o.x + d.x * entry_t, g.bmin[0]), g.bmax[0]),
+                               fminf(fmaxf(o.y + d.y * entry_t, g.bmin[1]), g.bmax[1]),
+                               fminf(fmaxf(o.z + d.z * entry_t, g.bmin[2]), g.bmax[2]));
+    int3 cell;
+    if (!cell_coordinate(start, d, g, cell)) return h;
+    int3 step = make_int3(0, 0, 0);
+    float3 next_t = make_float3(kInfF, kInfF, kInfF), delta_t = make_float3(kInfF, kInfF, kInfF);
+    for (int a = 0; a < 3; ++a) {
+        float da = axis(d, a), oa = axis(o, a);
+        float nt = kInfF, dt = kInfF;
+        if (da > 0.0f) {
+            set_iaxis(step, a, 1);
+            float boundary = g.bmin[a] + float(iaxis(cell, a) + 1) * g.cs[a];
+            nt = (boundary - oa) / da;
+            dt = g.cs[a] / da;
+        } else if (da < 0.0f) {
+            set_iaxis(step, a, -1);
+            float boundary = g.bmin[a] + float(iaxis(cell, a)) * g.cs[a];
+            nt = (boundary - oa) / da;
+            dt = -g.cs[a] / da;
+        }
+        if (!isfinite(nt) || !isfinite(dt)) { nt = kInfF; dt = kInfF; }
+        set_axis(next_t, a, nt);
+        set_axis(delta_t, a, dt);
+    }
+    int last_axis = -1;   // axis crossed by the last advance (-1: none yet, the normal is the box entry face)
+    const int r = int(g.res);
+    const uint32_t max_steps = g.res * 3u + 3u;
+    const uint32_t bg = g.brick_grid;
+    const unsigned long long *mask = reinterpret_cast<const unsigned long long *>(g.mask);
+    for (uint32_t s = 0; s < max_steps && entry_t <= far_t; ++s) {
+        if (cell.x < 0 || cell.y < 0 || cell.z < 0 || cell.x >= r || cell.y >= r || cell.z >= r) break;
+        const uint32_t x = uint32_t(cell.x), y = uint32_t(cell.y), z = uint32_t(cell.z);
+        const uint32_t page = __ldg(g.table + (x >> 3) + ((y >> 3) + (z >> 3) * bg) * bg);
+        if (page != 0u && ((__ldg(mask + size_t(page - 1u) * 8u + (z & 7u)) >> ((x & 7u) + 8u * (y & 7u))) & 1ull)) {
+            h.hit = true;
+            h.t = entry_t;
+            h.exit_t = fminf(next_t.x, fminf(next_t.y, next_t.z));
+            h.cell = cell;
+            if (last_axis >= 0) {
+                const int st = last_axis == 0 ? step.x : (last_axis == 1 ? step.y : step.z);
+                const float nv = st > 0 ? -1.0f : 1.0f;
+                h.normal = make_float3(last_axis == 0 ? nv : 0.0f, last_axis == 1 ? nv : 0.0f, last_axis == 2 ? nv : 0.0f);
+            } else {
+                h.normal = en;
+            }
+            h.steps = s + 1;
+            return h;
+        }
+        const float bt = fminf(next_t.x, fminf(next_t.y, next_t.z));
+        if (!isfinite(bt)) break;
+        const bool cx = next_t.x == bt, cy = next_t.y == bt, cz = next_t.z == bt;
+        float ne = bt;
+        if (!(ne > entry_t)) {
+            ne = next_positive_float(entry_t);
+            if (!isfinite(ne) || !(ne > entry_t)) break;
+        }
+        entry_t = ne;
+        last_axis = cx ? 0 : (cy ? 1 : 2);
+        if (cx) { cell.x += step.x; next_t.x = next_t.x + delta_t.x; }
+        if (cy) { cell.y += step.y; next_t.y = next_t.y + delta_t.y; }
+        if (cz) { cell.z += step.z; next_t.z = next_t.z + delta_t.z; }
+    }
+    return h;
+}
+
 }  // namespace vox
 }  // namespace fpt

@@ -31,8 +31,11 @@ namespace fpt {
 // box; the march classifies it as a miss without evaluating.  PF_KNOWN_D:
 // the skip pass handed the ray over with the exact distance at its position
 // in grad.w, so the march does not evaluate it again.
+// PF_FP64: the camera ray's hit came from the FP64 continuation; its FP64
+// distance from the camera is grad.w + shadow.w (high and low floats).
 enum PathFlags : uint32_t {
-    PF_DONE = 1u << 8, PF_INVISIBLE = 1u << 9, PF_VALID = 1u << 10, PF_ESCAPED = 1u << 11, PF_KNOWN_D = 1u << 12
+    PF_DONE = 1u << 8, PF_INVISIBLE = 1u << 9, PF_VALID = 1u << 10, PF_ESCAPED = 1u << 11, PF_KNOWN_D = 1u << 12,
+    PF_FP64 = 1u << 13
 };
 
 struct alignas(16) PathRec {
@@ -71,7 +74,9 @@ constexpr uint32_t C_CAMSTEP = 9;
 // Profile counters (FptSdfProfileStats): 0-2 march steps of primary /
 // secondary / shadow rays, 3 normal evaluations, 4 bounces, 5 finished paths,
 // 7 material evaluations, 8-10 orbit iterations of primary / secondary /
-// shadow rays, 11 refinement steps, 12 most steps of one march.
+// shadow rays, 11 refinement steps, 12 most steps of one march, 13 most
+// march steps of one path (all its rays: max_pixel_steps), 14 orbit
+// iterations of normal evaluations.
 constexpr int kProfileSlots = 16;
 // Lockstep march: finished lanes write their results and take new rays in
 // groups of this many (measured at 1080p 16 spp: 2 -> 863, 4 -> 923, 8 -> 944,
@@ -108,6 +113,7 @@ struct WaveParams {
     uint32_t tiles_x;
     uint32_t sample_begin, sample_count;
     unsigned long long *profile;   // kProfileSlots counters or null
+    uint32_t *path_steps;          // profile renders: march steps of each path of the wave (all its rays), or null
     // Box holding all geometry (surrogate modes): a march starts where its
     // ray enters the box and ends as a miss where it leaves it.
     uint32_t box_on;
@@ -317,7 +323,11 @@ struct MarchJob {
     float3 rp0;         // shadow: hit point the ray leaves
 };
 
-template <int KIND, bool BATCH = false, int BLOCK = 128, int MINB = 7>
+// FP64: the camera-ray pass of a deep-zoom scene (FptCudaSceneExt.fp64_bisection,
+// a pinhole camera): a camera ray whose FP32 march stopped because a step no
+// longer moved its position (shaders/Shaders.metal:3726, 3739-3746) continues
+// in FP64 (march_fp64), which decides hit or miss and the hit distance.
+template <int KIND, bool BATCH = false, int BLOCK = 128, int MINB = 7, bool FP64 = false>
 __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cur) {
     const DeviceScene *sp = W.scene;   // the lane's scene (per job when BATCH)
     const uint32_t n_path = W.counters[C_MARCH0 + cur];
@@ -467,6 +477,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
                 atomicMax(&s_prof[4], uint32_t(m.steps));
             }
             c_job_orbit = 0;
+            if (W.path_steps) atomicAdd(W.path_steps + job.path, uint32_t(m.steps));
             if (job.shadow) {
                 c_shadow += m.steps;
                 if (len3(job.rp0 - m.pos) > S.render[4] * 0.99f) {
@@ -476,6 +487,23 @@ __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cu
             } else {
                 if (job.bounce == 0u) c_primary += m.steps; else c_secondary += m.steps;
                 PathRec &R = W.paths[job.path];
+                if (FP64 && job.bounce == 0u && m.stalled) {
+                    // restart a few FP32 ulps before the stop (the FP32 position is only that accurate)
+                    const float back = 8.0f * 1.1920929e-7f * fmaxf(fmaxf(fabsf(m.pos.x), fabsf(m.pos.y)), fmaxf(fabsf(m.pos.z), 1.0f));
+                    double t64 = 0.0;
+                    int st = 0;
+                    const double t0 = fmax(double(len3(m.pos - box_origin)) - double(back), 0.0);
+                    if (march_fp64<KIND>(S, box_origin, m.dir, t0, int(S.render[1]), t64, st)) {
+                        m.pos = box_origin + normalize3(m.dir) * float(t64);
+                        const float hi = float(t64);
+                        R.grad.w = hi;
+                        R.shadow.w = float(t64 - double(hi));
+                        R.color.w = bitsf(fbits(R.color.w) | PF_FP64);
+                    } else {
+                        m.pos = m.pos + m.dir * (S.render[4] + len3(m.pos - cam) + 1.0f);   // no surface: a miss
+                    }
+                    c_primary += uint32_t(st);
+                }
                 float3 r = m.pos - cam;
                 float travel2 = dot(r, r);
                 float maxd = S.render[4], far = maxd * 0.99f;
@@ -556,7 +584,8 @@ template <int KIND, bool BATCH = false>
 __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
     const int next = cur ^ 1;
     const uint32_t n = W.counters[C_SHADE];
-    uint32_t c_normal = 0, c_material = 0, c_paths = 0, c_bounces = 0;
+    uint32_t c_normal = 0, c_material = 0, c_paths = 0, c_bounces = 0, c_normal_orbit = 0;
+    uint32_t *const normal_orbit = W.profile ? &c_normal_orbit : nullptr;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += gridDim.x * blockDim.x) {
         bool live = i < n;
         bool emit_march = false, emit_shadow = false;
@@ -587,10 +616,25 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
             Material mt;
             float3 nrm;
             c_material += 1;
-            if (S.formula != 0 && S.ext_normal == FPT_CUDA_NORMAL_ANALYTIC && S.fractal_style_mode == 0u && ggx) {
+            if (bounce == 0 && (state & PF_FP64)) {
+                // deep zoom: the normal at the FP64 hit point (the FP32 position is thresholds away from it)
+                const double t64 = double(R.grad.w) + double(R.shadow.w);
+                double dx = dr.x, dy = dr.y, dz = dr.z;
+                const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+                dx *= inv; dy *= inv; dz *= inv;
+                nrm = normal_fp64<KIND>(S, double(S.cam_pos[0]) + dx * t64, double(S.cam_pos[1]) + dy * t64,
+                                        double(S.cam_pos[2]) + dz * t64);
+                mt = material_of(S, scene_eval<KIND>(S, hit, EV_MATERIAL));
+                if (ggx) {
+                    mt = default_material();
+                    mt.rgb = mk3(S.albedo);
+                    mt.surface = 0;
+                }
+                c_normal += 6;
+            } else if (S.formula != 0 && S.ext_normal == FPT_CUDA_NORMAL_ANALYTIC && S.fractal_style_mode == 0u && ggx) {
                 // One dual-number evaluation gives the surface id and the gradient.
                 float3 g;
-                analytic_gradient<KIND>(S, hit, g);
+                analytic_gradient<KIND>(S, hit, g, normal_orbit);
                 int surface = 0;
                 if (S.ground_plane) {
                     Eval e = ext_eval<KIND>(S, hit);
@@ -603,7 +647,7 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
                 c_normal += 1;
             } else {
                 mt = material_of(S, scene_eval<KIND>(S, hit, EV_MATERIAL));
-                nrm = normal_direct<KIND>(hit, S);
+                nrm = normal_direct<KIND>(hit, S, normal_orbit);
                 c_normal += normal_is_analytic(S) ? 1u : uint32_t(tap_count(S));
             }
             if (mt.emission > 0.001f) light = light + (ggx ? mt.rgb * (mt.emission) * color : mt.rgb * mt.emission);
@@ -737,11 +781,11 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
         if (emit_shadow) W.q_shadow[next][sat] = J;
     }
     if (W.profile) {
-        uint32_t v[4] = {c_normal, c_material, c_paths, c_bounces};
-        const int slot[4] = {3, 7, 5, 4};
+        uint32_t v[5] = {c_normal, c_material, c_paths, c_bounces, c_normal_orbit};
+        const int slot[5] = {3, 7, 5, 4, 14};
         const unsigned FULL = 0xffffffffu;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 5; ++k) {
             uint32_t s = v[k];
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
             if ((threadIdx.x & 31u) == 0 && s) atomicAdd(W.profile + slot[k], (unsigned long long)s);
@@ -784,6 +828,11 @@ static __global__ void reset_counters_kernel(uint32_t *counters, int next) {
 template <bool BATCH>
 __global__ void __launch_bounds__(256) finalize_kernel(WaveParams W) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (W.path_steps) {   // profile renders: the largest march-step total of one path
+        uint32_t v = p < W.n_paths ? W.path_steps[p] : 0u;
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((threadIdx.x & 31u) == 0u && v) atomicMax(W.profile + 13, (unsigned long long)v);
+    }
     if (p >= W.n_paths) return;
     const PathRec &R = W.paths[p];
     uint32_t state = fbits(R.color.w);

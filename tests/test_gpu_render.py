@@ -138,8 +138,9 @@ def test_zero_bounces_is_background(native):
 
 def test_profile_stats(native):
     """FptSdfProfileStats of a profiled render (the counters the reference's render metadata reports,
-    src/main.rs:1491-1520): per-phase march steps and orbit iterations, refinement steps, the longest march,
-    and the render time apportioned by counted work units (src/metal_bridge.mm:5712-5733)."""
+    src/main.rs:1491-1520): per-phase march steps and orbit iterations (the normal phase included), refinement
+    steps, the longest march, the most march steps of one path, and the render time apportioned by counted work
+    units (src/metal_bridge.mm:5712-5733)."""
     b = scenes.mandelbulb_path(96, 64, 2, 4)
     _, _, ms, prof = native.cuda_render(b.cfg, b.ext, linear=False, profile=True)
     p = {f: getattr(prof, f) for f, _ in type(prof)._fields_}
@@ -148,13 +149,17 @@ def test_profile_stats(native):
     assert 0 < p["bounces"] <= p["normal_evals"] == p["material_evals"]
     assert p["distance_evals"] == p["primary_steps"] + p["secondary_steps"] + p["shadow_steps"]
     orbit = list(prof.orbit_iterations_by_phase)
-    assert p["march_orbit_iterations"] == orbit[0] + orbit[1] + orbit[2] > 0
+    assert p["march_orbit_iterations"] == orbit[0] + orbit[1] + orbit[2] + orbit[3] > 0
+    # one analytic (dual-number) normal per hit: 1..8 orbit iterations each
+    assert p["normal_evals"] <= orbit[3] <= 8 * p["normal_evals"]
     assert prof.formula_slot_iterations[0] == p["march_orbit_iterations"]
     # every evaluation runs 1..8 iterations of the power-8 Mandelbulb
     for k, steps in enumerate(("primary_steps", "secondary_steps", "shadow_steps")):
         assert p[steps] <= orbit[k] <= 8 * p[steps]
     assert 0 < p["refinement_steps"] == p["refinement_distance_evals"]
     assert 0 < p["max_ray_steps"] <= 256 + 30
+    # a path's steps over all its rays (camera, bounces, shadow rays): at least its longest ray, at most 9 rays' worth
+    assert p["max_ray_steps"] <= p["max_pixel_steps"] <= 9 * (256 + 30)
     est = p["primary_ms_estimate"] + p["secondary_ms_estimate"] + p["shadow_ms_estimate"] + p["normal_ms_estimate"] + \
         p["bounce_ms_estimate"]
     assert abs(est - ms) <= 1e-6 * ms + 1e-9
