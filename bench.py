@@ -225,7 +225,7 @@ def main():
     def series(e, steps, clocks=None):
         """Device-timed renders (library CUDA events) with L2 flushed before each; per-kernel spans recorded."""
         out = {"ms": [], "march_ms": 0.0, "march_launches": 0, "march_evals": 0, "skip_ms": 0.0, "shade_ms": 0.0,
-               "launches": 0}
+               "launches": 0, "phase_evals": None}
         for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -238,6 +238,7 @@ def main():
             out["skip_ms"] += rs["skip_ms"]
             out["shade_ms"] += rs["shade_ms"]
             out["launches"] += rs["kernel_launches"]
+            out["phase_evals"] = [int(prof.primary_steps), int(prof.secondary_steps), int(prof.shadow_steps)]
         return out
 
     # End-to-end through the public call: the results land in pinned host buffers (allocated once, reused).
@@ -267,6 +268,10 @@ def main():
     barrier()
     plain_e2e = e2e_series(ext, args.steps)
     barrier()
+    # ---- what a perfect proposal could save under the skip's certificate (per ray type, then weighted by the
+    # plain frame's evaluations per phase)
+    bound = nx.certified_step_bound(cfg, ext, list(ext.sun_direction), stride=4, margin=0.1)
+    bound0 = nx.certified_step_bound(cfg, ext, list(ext.sun_direction), stride=4, margin=0.0)
     # ---- learned skip: train once (outside the timed region), then render
     model, train = nx.mlp_create(cfg, ext, surrogate_config())
     skip_ext = ffi_copy(ext)
@@ -348,6 +353,7 @@ def main():
                  "skip_ms": skip["skip_ms"] / args.steps, "march_ms": skip["march_ms"] / args.steps,
                  "shade_ms": skip["shade_ms"] / args.steps, "train_ms": train["train_ms"], "data_ms": train["data_ms"],
                  "loss_first": train["loss_first"], "loss_last": train["loss_last"]},
+        "perfect_proposal_bound": frame_bound(bound, bound0, plain["phase_evals"]),
         "e2e": {"value": e2e, "unit": UNIT, "host_buffers": "pinned, allocated once",
                 "h2d_bytes_per_step": ctypes.sizeof(cfg) + ctypes.sizeof(ext),
                 "d2h_bytes_per_step": W * H * 16 + W * H * 4},
@@ -391,6 +397,20 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def frame_bound(bound, bound0, phase_evals):
+    """The most a perfect proposal could save on the frame: per ray type the ratio of plain to certified
+    evaluations (camera / bounce / shadow rays of a pixel sample), applied to the plain frame's evaluations of
+    primary / secondary / shadow rays; with the skip's hand-over margin 0.1 and with none."""
+    out = {"per_ray_type_margin_0.1": bound, "per_ray_type_margin_0": bound0}
+    if phase_evals:
+        e = phase_evals
+        for key, b in (("frame_bound_margin_0.1", bound), ("frame_bound_margin_0", bound0)):
+            cert = e[0] / b["camera"]["ratio"] + e[1] / b["bounce"]["ratio"] + e[2] / b["shadow"]["ratio"]
+            out[key] = sum(e) / cert
+        out["plain_frame_evals_by_phase"] = e
+    return out
 
 
 def other_configs(native, nx, scenes, peaks):

@@ -930,6 +930,36 @@ int fpt_test_typed_soa(const char *metallib_path, const struct FptRenderConfig *
     return 0;
 }
 
+int fpt_cuda_certified_steps(const struct FptRenderConfig *config, const struct FptCudaSceneExt *ext, uint32_t stride, float margin,
+                             const float *sun_direction, uint32_t *counts, size_t counts_len, char *error, size_t error_len) {
+    if (!config || !sun_direction || !counts || stride == 0 || config->width == 0 || config->height == 0) {
+        set_error(error, error_len, "missing certified-step input");
+        return 1;
+    }
+    const size_t samples = size_t((config->width + stride - 1) / stride) * ((config->height + stride - 1) / stride);
+    if (counts_len < samples * 6) { set_error(error, error_len, "counts buffer too small (%zu < %zu)", counts_len, samples * 6); return 1; }
+    const float sl = std::sqrt(sun_direction[0] * sun_direction[0] + sun_direction[1] * sun_direction[1] +
+                               sun_direction[2] * sun_direction[2]);
+    if (!(sl > 0.0f)) { set_error(error, error_len, "sun direction must be non-zero"); return 1; }
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    if (!ensure_device(error, error_len)) return 1;
+    Context &c = ctx();
+    DeviceScene S;
+    if (!compile_scene(*config, ext, S, error, error_len)) return 1;
+    S.surrogate = 0;   // the plain march's rules; no model is needed
+    if (!upload_scene(S, nullptr, error, error_len)) return 1;
+    if (!ensure_buffer((void **)&c.samples, &c.cap_samples, samples * 6 * sizeof(uint32_t), error, error_len)) return 1;
+    uint32_t *dev = reinterpret_cast<uint32_t *>(c.samples);
+    const float3 sun = make_float3(sun_direction[0] / sl, sun_direction[1] / sl, sun_direction[2] / sl);
+    if (!check(launch_certified_steps(S.kind, c.scene, uint32_t(samples), stride, margin, sun, dev, c.stream), "certified-step launch",
+               error, error_len) ||
+        !check(cudaMemcpyAsync(counts, dev, samples * 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream), "readback", error,
+               error_len) ||
+        !check(cudaStreamSynchronize(c.stream), "certified-step bound", error, error_len))
+        return 1;
+    return 0;
+}
+
 int fpt_cuda_measure_fp32_peak(double *tflops, double *launch_ms, char *error, size_t error_len) {
     if (tflops) *tflops = 0.0;
     if (launch_ms) *launch_ms = 0.0;

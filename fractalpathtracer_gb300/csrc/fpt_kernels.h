@@ -79,6 +79,9 @@ cudaError_t launch_diag_final(const DeviceScene *scene, uint32_t W, uint32_t H, 
 // Typed SoA vs interpreter over n hash-seeded points; counts[4] as in the kernel.
 cudaError_t launch_typed_soa_validation(const DeviceScene *scene, const float bmin[3], const float bmax[3], uint32_t n,
                                         unsigned int *counts, cudaStream_t stream);
+// Plain-march and perfect-proposal certified evaluations of camera, shadow and bounce rays of sampled pixels (6 per pixel).
+cudaError_t launch_certified_steps(uint32_t kind, const DeviceScene *scene, uint32_t samples, uint32_t stride, float margin, float3 sun,
+                                   uint32_t *counts, cudaStream_t stream);
 cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, const float4 *accum, uchar4 *out,
                            cudaStream_t stream);
 

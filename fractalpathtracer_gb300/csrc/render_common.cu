@@ -99,7 +99,8 @@ cudaError_t launch_present(const DeviceScene *scene, uint32_t W, uint32_t H, con
     cudaError_t launch_label_k##n(const DeviceScene *, float4 *, size_t, cudaStream_t);                                      \
     cudaError_t launch_diagnostic_k##n(const DeviceScene *, uint32_t, uint32_t, uint32_t, float, uchar4 *, cudaStream_t);     \
     cudaError_t launch_skip_primary_k##n(const DeviceScene *, uint32_t, uint32_t, const SkipArgs &, FptCudaPrimaryHit *,     \
-                                         cudaStream_t);
+                                         cudaStream_t);                                                                     \
+    cudaError_t launch_certified_steps_k##n(const DeviceScene *, uint32_t, uint32_t, float, float3, uint32_t *, cudaStream_t);
 FPT_DECLARE_KIND(0)
 FPT_DECLARE_KIND(1)
 FPT_DECLARE_KIND(2)
@@ -137,6 +138,10 @@ cudaError_t launch_diag_final(const DeviceScene *scene, uint32_t W, uint32_t H, 
 }
 cudaError_t launch_label(uint32_t kind, const DeviceScene *scene, float4 *pts, size_t n, cudaStream_t st) {
     FPT_DISPATCH(kind, launch_label_k, scene, pts, n, st)
+}
+cudaError_t launch_certified_steps(uint32_t kind, const DeviceScene *scene, uint32_t samples, uint32_t stride, float margin, float3 sun,
+                                   uint32_t *counts, cudaStream_t st) {
+    FPT_DISPATCH(kind, launch_certified_steps_k, scene, samples, stride, margin, sun, counts, st)
 }
 cudaError_t launch_skip_primary(uint32_t kind, const DeviceScene *scene, uint32_t W, uint32_t H, const SkipArgs &args,
                                 FptCudaPrimaryHit *hits, cudaStream_t st) {

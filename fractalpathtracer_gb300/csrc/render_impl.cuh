@@ -70,6 +70,101 @@ __global__ void __launch_bounds__(128) trace_primary_kernel(const DeviceScene *s
     hits[size_t(gy) * S.width + gx] = h;
 }
 
+// ---------------------------------------------------------------- certified-step bound
+// What any distance proposal can save under the certificate of the surrogate
+// skip (a step s from p is taken when s <= DE(p) + DE(p + s dir): the two
+// empty balls overlap).  Per ray: the plain march's evaluations, and the
+// evaluations of a march that always takes the longest step the certificate
+// allows -- found by a search along the ray whose evaluations are not
+// counted (a perfect proposal) -- until the distance falls under the hand-over
+// margin, after which the plain march finishes the ray from there.
+template <int KIND>
+__device__ float longest_certified_step(const DeviceScene &S, float3 p, float3 dir, float d, float limit) {
+    auto ok = [&](float s) {
+        const float e = scene_eval<KIND>(S, p + dir * s, EV_MAP).d;
+        return isfinite(e) && s <= d + e;
+    };
+    float lo = 0.0f, hi = fminf(d, limit);
+    for (int k = 0; k < 24 && hi <= limit && ok(hi); ++k) { lo = hi; hi *= 2.0f; }
+    if (lo >= limit) return limit;
+    hi = fminf(hi, limit);
+    for (int k = 0; k < 12; ++k) {
+        const float mid = 0.5f * (lo + hi);
+        if (ok(mid)) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Plain and certified evaluations of one ray (counts[0], counts[1]).
+template <int KIND>
+__device__ void certified_ray(const DeviceScene &S, float3 o, float3 dir, float margin, uint32_t *counts) {
+    const int ni = int(S.render[1]);
+    counts[0] = uint32_t(march_loop<KIND>(S, o, dir, ni, S.render[3], 0.0002f).steps);
+    float3 p = o;
+    float travel = 0.0f, last = 0.0f;
+    int steps = 0;
+    uint32_t counted = 0;
+    const int maxi = march_iteration_limit(ni, S);
+    while (steps < maxi) {
+        const float d = scene_eval<KIND>(S, p, EV_MAP).d;   // one counted evaluation per position stood on
+        ++counted;
+        const float th = S.sdf_id == FPT_SDF_MANDELBULBER ? mandel_threshold(p, S) : S.render[3];
+        if (!isfinite(d) || d < fmaxf(margin, 4.0f * th)) break;   // the plain march finishes the ray
+        const float limit = S.render[4] - travel;
+        if (!(limit > 0.0f)) break;
+        const float step = longest_certified_step<KIND>(S, p, dir, d, limit);
+        if (!(step > 0.0f)) break;
+        p = p + dir * step;
+        travel += step;
+        last = step;
+        ++steps;
+        if (travel >= S.render[4]) break;
+    }
+    if (travel < S.render[4] && steps < maxi) {
+        // resume the plain march at p (its first evaluation repeats the one just counted)
+        const March m = march_loop_from<KIND>(S, o, p, dir, ni, S.render[3], 0.0002f, steps, last);
+        counted += uint32_t(m.steps > 0 ? m.steps - 1 : 0);
+    }
+    counts[1] = counted;
+}
+
+// Per sampled pixel (every `stride`-th pixel centre): counts[6] = plain and
+// certified evaluations of the camera ray, of its hit's sun shadow ray (when
+// the sun is above the surface) and of one cosine-distributed bounce ray, the
+// secondary rays starting 0.001 off the surface along the normal as the path
+// tracer starts them (zeros where a ray does not exist).
+template <int KIND>
+__global__ void __launch_bounds__(128) certified_steps_kernel(const DeviceScene *scene, uint32_t stride, float margin, float3 sun,
+                                                              uint32_t *counts) {
+    const DeviceScene &S = *scene;
+    const uint32_t cols = (S.width + stride - 1u) / stride, rows = (S.height + stride - 1u) / stride;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cols * rows) return;
+    uint32_t *c = counts + size_t(i) * 6;
+    for (int k = 0; k < 6; ++k) c[k] = 0u;
+    const uint32_t gx = (i % cols) * stride, gy = (i / cols) * stride;
+    const float2 uv = screen_uv(gx, gy, S);
+    PathRng rng;
+    rng.init(false, 0u, 0u, 0u, uv.x, uv.y);
+    float3 rp, dr;
+    if (!camera_ray(S, uv, rng, false, rp, dr)) return;
+    certified_ray<KIND>(S, rp, dr, margin, c);
+    const March m = march_loop<KIND>(S, rp, dr, int(S.render[1]), S.render[3], 0.0002f);
+    const float travel = len3(m.pos - rp);
+    if (!(m.found && isfinite(travel) && travel < S.render[4] * 0.99f)) return;
+    float3 n = normal_direct<KIND>(m.pos, S);
+    if (dot(n, dr) > 0.0f) n = -n;
+    const float3 o = m.pos + n * 0.001f;
+    if (dot(n, sun) > 0.0f) certified_ray<KIND>(S, o, sun, margin, c + 2);
+    const uint32_t h1 = pcg_hash(i * 2u + 0x9e3779b9u), h2 = pcg_hash(i * 2u + 1u + 0x7f4a7c15u);
+    const float u1 = float(h1 >> 8) * (1.0f / 16777216.0f), u2 = float(h2 >> 8) * (1.0f / 16777216.0f);
+    const float3 a = fabsf(n.x) > 0.9f ? mk3(0.0f, 1.0f, 0.0f) : mk3(1.0f, 0.0f, 0.0f);
+    const float3 t = normalize3(cross3(n, a)), b = cross3(n, t);
+    const float r = sqrtf(u1), ph = 6.28318530718f * u2;
+    const float3 bd = normalize3(t * (r * cosf(ph)) + b * (r * sinf(ph)) + n * sqrtf(fmaxf(0.0f, 1.0f - u1)));
+    certified_ray<KIND>(S, o, bd, margin, c + 4);
+}
+
 // ---------------------------------------------------------------- focus prepass
 // estimate_focus_distance_kernel (shaders/Shaders.metal:5869-5884): one
 // thread writes the resolved focus into the scene block in device memory.

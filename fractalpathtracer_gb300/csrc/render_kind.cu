@@ -161,6 +161,11 @@ cudaError_t FPT_CAT(launch_diagnostic_k, FPT_KIND)(const DeviceScene *scene, uin
     diagnostic_kernel<FPT_KIND><<<grid, 128, 0, st>>>(scene, mode, max_distance, 0u, 0u, out);
     return cudaGetLastError();
 }
+cudaError_t FPT_CAT(launch_certified_steps_k, FPT_KIND)(const DeviceScene *scene, uint32_t samples, uint32_t stride, float margin,
+                                                        float3 sun, uint32_t *counts, cudaStream_t st) {
+    certified_steps_kernel<FPT_KIND><<<(samples + 127u) / 128u, 128, 0, st>>>(scene, stride, margin, sun, counts);
+    return cudaGetLastError();
+}
 #if FPT_KIND == 0
 cudaError_t launch_field_sample(const DeviceScene *scene, const float4 *pts, float4 *out, size_t n, cudaStream_t st) {
     unsigned blocks = unsigned((n + 255) / 256);

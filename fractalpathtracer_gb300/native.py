@@ -30,7 +30,7 @@ EXPORTED = [
     "fpt_test_bounded_waits",
     "fpt_cuda_set_loop_limit",
     "fpt_cuda_set_device", "fpt_cuda_get_device", "fpt_cuda_hdri_lut",
-    "fpt_cuda_measure_fp32_peak",
+    "fpt_cuda_measure_fp32_peak", "fpt_cuda_certified_steps",
 ]
 
 
@@ -79,6 +79,7 @@ def _declare(L: C.CDLL) -> None:
     L.fpt_cuda_set_device.argtypes = [C.c_int32]
     L.fpt_cuda_hdri_lut.argtypes = [C.c_char_p, P(C.c_uint16), C.c_size_t] + err
     L.fpt_cuda_measure_fp32_peak.argtypes = [P(C.c_double), P(C.c_double)] + err
+    L.fpt_cuda_certified_steps.argtypes = [cfg, ext, C.c_uint32, C.c_float, P(C.c_float), P(C.c_uint32), C.c_size_t] + err
     L.fpt_cuda_get_device.argtypes = [P(C.c_int32)]
     for name in EXPORTED:
         getattr(L, name).restype = C.c_int
@@ -211,6 +212,18 @@ def compare_images(baseline: str, candidate: str, report: str) -> dict:
         _raise(e)
     with open(report) as f:
         return json.load(f)
+
+
+def certified_steps(config, ext, sun_direction, stride: int = 4, margin: float = 0.1) -> np.ndarray:
+    """fpt_cuda_certified_steps: (samples, 6) plain / certified evaluations of camera, shadow and bounce rays."""
+    samples = ((config.width + stride - 1) // stride) * ((config.height + stride - 1) // stride)
+    out = np.zeros(samples * 6, np.uint32)
+    sun = np.ascontiguousarray(sun_direction, np.float32)
+    e = _err()
+    if lib().fpt_cuda_certified_steps(C.byref(config), C.byref(ext) if ext is not None else None, stride, float(margin),
+                                      _ptr(sun, C.c_float), _ptr(out, C.c_uint32), out.size, e, len(e)) != 0:
+        _raise(e)
+    return out.reshape(samples, 6)
 
 
 def measure_fp32_peak() -> dict:

@@ -344,3 +344,16 @@ def set_march_schedule(schedule: int = 0, batch: int = 0) -> None:
     from .native import lib
     if lib().fpt_cuda_set_march_schedule(schedule, batch) != 0:
         raise ValueError("schedule must be 0 and batch 0..32")
+
+
+def certified_step_bound(cfg, ext, sun_direction, stride: int = 4, margin: float = 0.1) -> dict:
+    """Perfect-proposal bound of the surrogate skip per ray type (fpt_cuda_certified_steps): plain-march and
+    certified evaluations of camera, sun shadow and bounce rays of every `stride`-th pixel, and their ratio."""
+    from . import native
+    c = native.certified_steps(cfg, ext, sun_direction, stride, margin).astype(np.int64)
+    out = {}
+    for k, name in enumerate(("camera", "shadow", "bounce")):
+        plain, cert = int(c[:, 2 * k].sum()), int(c[:, 2 * k + 1].sum())
+        out[name] = {"rays": int((c[:, 2 * k] > 0).sum()), "plain_evals": plain, "certified_evals": cert,
+                     "ratio": plain / max(cert, 1)}
+    return out

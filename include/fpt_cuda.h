@@ -859,6 +859,30 @@ int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
  * depend on either. */
 int fpt_cuda_set_launch_shape(uint32_t wave_paths, int32_t march_blocks);
 
+/* The bound a perfect distance proposal puts on the surrogate skip (no
+ * counterpart in the reference).  For every `stride`-th pixel centre of the
+ * config's image, counts gets six numbers: the distance evaluations of the
+ * plain march and of a "certified" march for the camera ray, for the sun
+ * shadow ray of its hit (toward sun_direction, when the sun is above the
+ * surface) and for one cosine-distributed bounce ray of that hit (secondary
+ * rays start 0.001 off the surface along the normal, as the path tracer starts
+ * them; zeros where a ray does not exist).  The certified march stands on each
+ * position once and always takes the longest step the skip's certificate
+ * allows (s <= DE(p) + DE(p + s dir)) -- found by a search along the ray that
+ * is not counted, i.e. a perfect proposal -- until the distance falls under
+ * max(margin, 4 x the hit threshold); the plain march finishes the ray from
+ * there.  Plain over certified is the most any proposal can save.
+ * counts_len >= 6 x ceil(width / stride) x ceil(height / stride). */
+int fpt_cuda_certified_steps(const struct FptRenderConfig *config,
+                             const struct FptCudaSceneExt *ext,
+                             uint32_t stride,
+                             float margin,
+                             const float *sun_direction,
+                             uint32_t *counts,
+                             size_t counts_len,
+                             char *error,
+                             size_t error_len);
+
 /* Measured FP32 throughput of this device: a kernel of independent FMA chains
  * (2048 threads per SM) timed with CUDA events, best of six launches after two
  * warm-ups, about 2 ms each.  tflops = 2 x FMAs / time; launch_ms (optional)

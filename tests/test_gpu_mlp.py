@@ -240,3 +240,23 @@ def test_bounded_mbarrier_wait(blank_model):
     nx.set_network_engine(nx.NET_TCGEN05)
     y = nx.mlp_predict(blank_model, _points(256, 7))
     assert np.isfinite(y).all()
+
+
+@pytest.mark.parametrize("scene", ["mandelbulb", "mandelbox"])
+def test_perfect_proposal_bound(native, scene):
+    """fpt_cuda_certified_steps: in total a perfect proposal needs no more evaluations than the plain march for
+    camera, shadow and bounce rays; the ratio is the most any network can save under the skip's certificate.  Per
+    ray it is not monotone (measured: 1.4% of the Mandelbulb's and 4.4% of the Mandelbox's camera rays take more):
+    a longer certified step leaves the ray at another position, from which the remaining march can take longer."""
+    b = scenes.mandelbulb_path(480, 270, 1) if scene == "mandelbulb" else scenes.mandelbox_path(480, 270, 1)
+    c = native.certified_steps(b.cfg, b.ext, list(b.ext.sun_direction), stride=2, margin=0.1).astype(np.int64)
+    bound = nx.certified_step_bound(b.cfg, b.ext, list(b.ext.sun_direction), stride=2, margin=0.0)
+    print(scene, bound)
+    for k in range(3):
+        plain, cert = c[:, 2 * k], c[:, 2 * k + 1]
+        has = plain > 0
+        assert has.sum() > 100
+        assert cert[has].sum() <= plain[has].sum()
+        assert np.mean(cert[has] <= plain[has] + 1) > 0.9
+    for k in ("camera", "shadow", "bounce"):
+        assert bound[k]["ratio"] >= 1.0
