@@ -5,13 +5,20 @@
 // `near_band` of the surface (rejection sampling on the GPU).  Loss:
 // asymmetric squared error, overestimates weighted by `overestimate_weight`.
 // Optimiser: Adam on an FP32 master copy; BF16 weights and activations in the
-// tensor-core passes (mma.sync m16n8k16, FP32 accumulate):
-//   train_fwd_bwd_kernel   per warp 32 samples: forward through the 4 hidden
-//                          layers, loss, backward deltas (W products through
-//                          transposed ldmatrix); writes features,
-//                          activations, pre-activations and deltas (bf16)
-//   wgrad_kernel           dW_l = dZ_{l+1}^T H_l, split-K over the batch
-//   bias_grad_kernel, adam_kernel
+// tensor-core passes (FP32 accumulate):
+//   train_fwd_bwd_kernel   per warp 32 samples (mma.sync m16n8k16): forward
+//                          through the 4 hidden layers, loss, backward deltas
+//                          (W products through transposed ldmatrix); writes
+//                          features, activations, pre-activations and deltas
+//                          (bf16), and per warp its output-layer gradient and
+//                          loss sums
+//   wgrad_tc_kernel        tcgen05: per (layer, 512-row chunk of the batch)
+//                          D = H^T dZ, a 128 x 64 FP32 accumulator in tensor
+//                          memory; a row of ones in H^T gives the bias
+//                          gradient in the same MMAs
+//   wgrad_reduce_kernel,   the chunks' and warps' partial sums added in a
+//   out_reduce_kernel      fixed order: gradients and loss are deterministic
+//   adam_kernel
 // The skip march that uses the model is in skip.cuh (one instantiation per
 // scene kind).
 #include <cuda_bf16.h>
@@ -37,6 +44,7 @@ namespace mlp {
 
 constexpr int kWarpsTrain = 4;                 // 128 samples per block
 constexpr uint32_t kRowsPerBlock = 32u * kWarpsTrain;
+constexpr uint32_t kOutPart = kHid + 2;        // per warp of the training kernel: dW4[64], db4, loss
 
 // Shared scratch of one warp in the training kernel.
 struct WarpTrain {
@@ -58,8 +66,11 @@ struct TrainArgs {
     __nv_bfloat16 *gh[3];      // H1..H3 [rows x kHid]
     __nv_bfloat16 *gz[4];      // Z1..Z4 [rows x kHid]
     __nv_bfloat16 *gdz[4];     // dZ1..dZ4 [rows x kHid]
-    float *grad;               // kParams gradients (W4 and b4 accumulated here)
-    float *loss;               // sum of the batch loss
+    float *grad;               // kParams gradients (accumulated)
+    float *loss;               // sum of the batch loss (accumulated)
+    float *out_part;           // per warp kOutPart partial sums (output layer and loss)
+    float *w_part;             // wgrad_tc_kernel partials
+    uint32_t *fail;            // MMA time-out word of the tensor-core passes
 };
 
 __device__ __forceinline__ uint32_t hash2(uint32_t a, uint32_t b) { return pcg_hash(a ^ pcg_hash(b)); }
@@ -150,17 +161,21 @@ __global__ void __launch_bounds__(32 * kWarpsTrain, 2) train_fwd_bwd_kernel(Trai
     const float dout = valid ? 2.0f * wgt * e / float(A.batch) : 0.0f;
     float loss = valid ? wgt * e * e : 0.0f;
     for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
-    if (lane == 0) atomicAdd(A.loss, loss);
-    // output layer: dW4[j] = sum_b dout_b H4[b][j], db4 = sum_b dout_b
+    // output layer: dW4[j] = sum_b dout_b H4[b][j], db4 = sum_b dout_b; the warp's sums go to its
+    // partial row (out_reduce_kernel adds the warps in order)
+    float *part = A.out_part + size_t(blockIdx.x * kWarpsTrain + warp) * kOutPart;
     for (int j = 0; j < kHid; ++j) {
         float v = dout * __bfloat162float(h4[j]);
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) atomicAdd(A.grad + kW4 + j, v);
+        if (lane == 0) part[j] = v;
     }
     {
         float v = dout;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) atomicAdd(A.grad + kB4, v);
+        if (lane == 0) {
+            part[kHid] = v;
+            part[kHid + 1] = loss;
+        }
     }
     __syncwarp();   // Z4 rows written by other lanes are visible from here
     // dZ4 = dout W4 o SiLU'(Z4)
@@ -182,77 +197,159 @@ __global__ void __launch_bounds__(32 * kWarpsTrain, 2) train_fwd_bwd_kernel(Trai
     }
 }
 
-// dW[n][k] += sum_b dZ[b][n] H[b][k] over one chunk of the batch.  Block:
-// 4 warps, warp w owns columns col0 + 32 w .. + 31 of all 64 rows of dW
-// (4 m-tiles x 4 n-tiles); grid.x = batch chunks, grid.y = column blocks.
-constexpr int kChunk = 512;
-constexpr int kStrideWg = 128 + 8;
-__global__ void __launch_bounds__(128) wgrad_kernel(const __nv_bfloat16 *dz, const __nv_bfloat16 *h, int kcols, uint32_t batch,
-                                                    float *dw) {
-    __shared__ __align__(16) __nv_bfloat16 sdz[16 * kStrideH];
-    __shared__ __align__(16) __nv_bfloat16 sh[16 * kStrideWg];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int col0 = blockIdx.y * 128;
-    const int my_col = col0 + warp * 32;
-    float acc[4][4][4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int n = 0; n < 4; ++n)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.0f;
-    const uint32_t b0 = blockIdx.x * kChunk, b1 = min(batch, b0 + kChunk);
-    for (uint32_t kb = b0; kb < b1; kb += 16) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < 16 * 32; i += 128) {   // 16 rows x 64 columns as bf16 pairs
-            int r = i >> 5, c = (i & 31) * 2;
-            __nv_bfloat162 v = __floats2bfloat162_rn(0.0f, 0.0f);
-            if (kb + r < b1) v = *reinterpret_cast<const __nv_bfloat162 *>(dz + size_t(kb + r) * kHid + c);
-            *reinterpret_cast<__nv_bfloat162 *>(sdz + r * kStrideH + c) = v;
-        }
-        for (int i = threadIdx.x; i < 16 * 64; i += 128) {
-            int r = i >> 6, c = (i & 63) * 2;
-            __nv_bfloat162 v = __floats2bfloat162_rn(0.0f, 0.0f);
-            if (kb + r < b1 && col0 + c < kcols) v = *reinterpret_cast<const __nv_bfloat162 *>(h + size_t(kb + r) * kcols + col0 + c);
-            *reinterpret_cast<__nv_bfloat162 *>(sh + r * kStrideWg + c) = v;
-        }
-        __syncthreads();
-        if (my_col < kcols) {
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                uint32_t a[4];
-                load_a_trans(a, sdz, kStrideH, m * 16, 0, lane);   // A(n, b) = dZ[b][n]
-#pragma unroll
-                for (int n = 0; n < 4; ++n) {
-                    uint32_t b[2];
-                    load_b_kn(b, sh, kStrideWg, warp * 32 + n * 8, 0, lane);   // B(b, k) = H[b][k]
-                    mma16816(acc[m][n], a, b);
-                }
-            }
-        }
-    }
-    if (my_col >= kcols) return;
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int n = 0; n < 4; ++n)
-#pragma unroll
-            for (int hh = 0; hh < 2; ++hh) {
-                int r = m * 16 + g + hh * 8, c = my_col + n * 8 + t * 2;
-                if (c < kcols) atomicAdd(dw + size_t(r) * kcols + c, acc[m][n][hh * 2]);
-                if (c + 1 < kcols) atomicAdd(dw + size_t(r) * kcols + c + 1, acc[m][n][hh * 2 + 1]);
-            }
+// ---------------------------------------------------------------- weight gradients on tcgen05
+// For layer l and a chunk of the batch: D[m][n] = sum_b H_l[b][m] dZ_l[b][n]
+// (m < K_l: dW_l[n][m]; m = K_l: a row of ones in H^T, so D[K_l][n] is the
+// bias gradient db_l[n]).  A = H^T (128 x 64-row tile of the batch, K-major),
+// B = dZ^T (64 x 64), the M = 128, N = 64, K = 16 MMA shape of the forward
+// pass, accumulated over the chunk in one 64-column tensor-memory tile.  Each
+// CTA writes its 128 x 64 partial; wgrad_reduce_kernel adds the chunks in
+// order (no atomics: the same data gives the same bits).
+constexpr uint32_t kWgChunk = 512;            // batch rows per CTA
+constexpr uint32_t kWgTile = 64;              // batch rows per round of 4 MMAs
+struct WgSmem {
+    alignas(128) unsigned char a[kTcRows * kWgTile * 2];   // H^T tile, [k chunk][m group][8 m][8 k]
+    alignas(128) unsigned char b[kHid * kWgTile * 2];      // dZ^T tile, [k chunk][n group][8 n][8 k]
+    uint32_t tmem;
+    alignas(8) uint64_t bar;
+    unsigned char slack[4096];                             // keeps descriptor reads inside the CTA's shared memory
+};
+inline size_t wgrad_smem_bytes() { return sizeof(WgSmem); }
+
+struct WgradArgs {
+    const __nv_bfloat16 *h[kHidden];     // H_0 = features (kInPad columns), H_1..H_3 (kHid columns)
+    const __nv_bfloat16 *dz[kHidden];    // dZ_1..dZ_4 (kHid columns)
+    uint32_t batch, chunks;
+    float *part;                         // [layer][chunk][128][64] partial sums
+    uint32_t *fail;                      // set (bit 2) when an MMA does not complete in time; later launches skip their work
+};
+
+__device__ __forceinline__ uint32_t bf16_pair(float lo, float hi) {
+    return uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(lo))) | (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(hi))) << 16);
 }
 
-__global__ void __launch_bounds__(256) bias_grad_kernel(const __nv_bfloat16 *dz, uint32_t batch, float *db) {
-    __shared__ float part[256];
-    const int col = threadIdx.x & 63, sub = threadIdx.x >> 6;
-    float s = 0.0f;
-    for (uint32_t b = blockIdx.x * 4u + sub; b < batch; b += gridDim.x * 4u) s += __bfloat162float(dz[size_t(b) * kHid + col]);
-    part[threadIdx.x] = s;
+__global__ void __launch_bounds__(kTcRows) wgrad_tc_kernel(WgradArgs G) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    WgSmem &sm = *reinterpret_cast<WgSmem *>(smem_raw);
+    const int t = threadIdx.x;
+    const int layer = blockIdx.y;
+    const int kcols = layer == 0 ? kInPad : kHid;
+    const __nv_bfloat16 *H = G.h[layer], *DZ = G.dz[layer];
+    float *out = G.part + ((size_t(layer) * G.chunks + blockIdx.x) * kTcRows + uint32_t(t)) * kHid;
+    // an earlier launch gave up: no MMA here (one read, the same decision in every thread)
+    if (__syncthreads_or(t == 0 && *reinterpret_cast<volatile uint32_t *>(G.fail) != 0u)) {
+        for (int n = 0; n < kHid; ++n) out[n] = 0.0f;
+        return;
+    }
+    if (t == 0) umma::mbar_init(&sm.bar, 1u);
+    if (t < 32) {
+        __syncwarp();
+        umma::tmem_alloc(&sm.tmem, kTcCols);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x < 64) atomicAdd(db + col, part[col] + part[col + 64] + part[col + 128] + part[col + 192]);
+    umma::fence_after_sync();
+    const uint32_t a = umma::smem_u32(sm.a), bt = umma::smem_u32(sm.b);
+    const uint32_t b0 = blockIdx.x * kWgChunk, b1 = min(G.batch, b0 + kWgChunk);
+    uint32_t phase = 0;
+    bool fail = false, any = false;
+    for (uint32_t kb = b0; kb < b1; kb += kWgTile) {   // the same trips in every thread
+        // A: thread t holds column m = t of H^T (row t of the tile), 8 batch rows per 16-byte store
+#pragma unroll 1
+        for (int kc = 0; kc < int(kWgTile / 8); ++kc) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float v[2];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const uint32_t r = kb + uint32_t(kc * 8 + q * 2 + e);
+                    v[e] = r >= b1 ? 0.0f : (t < kcols ? __bfloat162float(H[size_t(r) * kcols + t]) : (t == kcols ? 1.0f : 0.0f));
+                }
+                w[q] = bf16_pair(v[0], v[1]);
+            }
+            umma::st_shared_v4(a + act_offset(t, kc), w[0], w[1], w[2], w[3]);
+        }
+        // B: thread t holds neuron n = t % 64 for half of the tile's batch rows
+        {
+            const int n = t & (kHid - 1), kc0 = (t >> 6) * int(kWgTile / 16);
+#pragma unroll 1
+            for (int kc = kc0; kc < kc0 + int(kWgTile / 16); ++kc) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t r = kb + uint32_t(kc * 8 + q * 2);
+                    const float v0 = r < b1 ? __bfloat162float(DZ[size_t(r) * kHid + n]) : 0.0f;
+                    const float v1 = r + 1 < b1 ? __bfloat162float(DZ[size_t(r + 1) * kHid + n]) : 0.0f;
+                    w[q] = bf16_pair(v0, v1);
+                }
+                umma::st_shared_v4(bt + w_core_offset(n, kc * 8), w[0], w[1], w[2], w[3]);
+            }
+        }
+        umma::fence_smem_to_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (t == 0) {
+            umma::fence_after_sync();
+#pragma unroll
+            for (uint32_t j = 0; j < kWgTile / 16; ++j)
+                umma::mma_bf16(sm.tmem, umma::smem_desc(a + j * 2u * kActK, kActK, kCore), umma::smem_desc(bt + j * 2u * kWK, kWK, kCore),
+                               kTcIdesc, (any || j > 0u) ? 1u : 0u);
+            umma::mma_commit(&sm.bar);
+        }
+        const int late = t == 0 ? int(!umma::mbar_wait(&sm.bar, phase, kMmaWaitNs)) : 0;
+        phase ^= 1u;
+        any = true;
+        if (__syncthreads_or(late)) {
+            fail = true;
+            break;
+        }
+        umma::fence_after_sync();
+    }
+    if (any && !fail) {
+        __syncwarp();
+        uint32_t r[64];
+        umma::tmem_ld64(sm.tmem + (uint32_t(t & ~31) << 16), r);
+#pragma unroll
+        for (int n = 0; n < kHid; n += 4)
+            *reinterpret_cast<float4 *>(out + n) = make_float4(__uint_as_float(r[n]), __uint_as_float(r[n + 1]), __uint_as_float(r[n + 2]),
+                                                               __uint_as_float(r[n + 3]));
+    } else {
+        for (int n = 0; n < kHid; ++n) out[n] = 0.0f;
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (t < 32) {
+        __syncwarp();
+        umma::fence_after_sync();
+        umma::tmem_dealloc(sm.tmem, kTcCols);
+    }
+    if (fail && t == 0) atomicOr(G.fail, 2u);
+}
+
+// grad += the chunks' partials, added in chunk order: one thread per (layer, m <= K_l, n).
+__global__ void __launch_bounds__(256) wgrad_reduce_kernel(const float *part, uint32_t chunks, float *grad) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= uint32_t(kHidden) * kTcRows * kHid) return;
+    const int layer = int(idx / (kTcRows * kHid)), m = int((idx / kHid) % kTcRows), n = int(idx % kHid);
+    const int kcols = k_of(layer);
+    if (m > kcols) return;
+    float s = 0.0f;
+    for (uint32_t c = 0; c < chunks; ++c) s += part[((size_t(layer) * chunks + c) * kTcRows + m) * kHid + n];
+    if (m < kcols) grad[w_offset(layer) + n * kcols + m] += s;
+    else grad[b_offset(layer) + n] += s;
+}
+
+// Output layer and loss: grad[W4], grad[b4] and the loss += the warps' partial sums, added in warp order.
+__global__ void __launch_bounds__(128) out_reduce_kernel(const float *part, uint32_t warps, float *grad, float *loss) {
+    const uint32_t j = threadIdx.x;
+    if (j >= kOutPart) return;
+    float s = 0.0f;
+    for (uint32_t w = 0; w < warps; ++w) s += part[size_t(w) * kOutPart + j];
+    if (j < uint32_t(kHid)) grad[kW4 + j] += s;
+    else if (j == uint32_t(kHid)) grad[kB4] += s;
+    else *loss += s;
 }
 
 __global__ void __launch_bounds__(256) adam_kernel(float *params, float *m, float *v, float *grad, __nv_bfloat16 *wbf, float lr,
@@ -383,6 +480,7 @@ struct HostModel {
     float4 *data = nullptr;
     uint32_t n_data = 0;
     __nv_bfloat16 *act = nullptr;   // gx | gh[3] | gz[4] | gdz[4]
+    float *part = nullptr;          // gradient partials: wgrad_tc_kernel chunks, then train-kernel warps, then the fail word
     uint32_t rows_cap = 0;
     float center[3] = {0, 0, 0}, inv_half[3] = {1, 1, 1}, lo[3] = {-1, -1, -1}, hi[3] = {1, 1, 1}, label_scale = 1.0f;
     uint32_t step = 0;
@@ -404,8 +502,16 @@ static uint64_t g_next_model = 1;
 
 static void free_model(HostModel *hm) {
     cudaFree(hm->params); cudaFree(hm->m); cudaFree(hm->v); cudaFree(hm->grad); cudaFree(hm->loss); cudaFree(hm->wbf);
-    cudaFree(hm->data); cudaFree(hm->act);
+    cudaFree(hm->data); cudaFree(hm->act); cudaFree(hm->part);
     delete hm;
+}
+
+// Partial sums of a batch of `rows`: [4 layers][chunks][128][64] for the
+// weight gradients, [warps][kOutPart] for the output layer and loss, and one
+// word for MMA time-outs.
+static uint32_t wgrad_chunks(uint32_t rows) { return (rows + kWgChunk - 1) / kWgChunk; }
+static size_t part_floats(uint32_t rows) {
+    return size_t(kHidden) * wgrad_chunks(rows) * kTcRows * kHid + size_t(rows / 32u) * kOutPart + 4;
 }
 
 static bool ensure_rows(HostModel &hm, uint32_t batch, char *error, size_t error_len) {
@@ -414,10 +520,30 @@ static bool ensure_rows(HostModel &hm, uint32_t batch, char *error, size_t error
     cudaFree(hm.act);
     hm.act = nullptr;
     hm.rows_cap = 0;
+    cudaFree(hm.part);
+    hm.part = nullptr;
     const size_t elems = size_t(rows) * (kInPad + 11 * kHid);
     if (!check(cudaMalloc(&hm.act, elems * sizeof(__nv_bfloat16)), "activation buffers", error, error_len)) return false;
+    if (!check(cudaMalloc(&hm.part, part_floats(rows) * sizeof(float)), "gradient partials", error, error_len) ||
+        !check(cudaMemset(hm.part, 0, part_floats(rows) * sizeof(float)), "gradient partials", error, error_len))
+        return false;
     hm.rows_cap = rows;
     return true;
+}
+
+// The MMA time-out word of the model's gradient passes (0: none timed out).
+static bool gradients_failed(const HostModel &hm, cudaStream_t st, char *error, size_t error_len) {
+    if (!hm.part) return false;
+    const float *w = hm.part + size_t(kHidden) * wgrad_chunks(hm.rows_cap) * kTcRows * kHid + size_t(hm.rows_cap / 32u) * kOutPart;
+    uint32_t f = 0;
+    if (!check(cudaMemcpyAsync(&f, w, 4, cudaMemcpyDeviceToHost, st), "gradient status readback", error, error_len) ||
+        !check(cudaStreamSynchronize(st), "gradient status readback", error, error_len))
+        return true;
+    if (f != 0u) {
+        set_error(error, error_len, "a weight-gradient MMA did not complete within 1 s (training aborted)");
+        return true;
+    }
+    return false;
 }
 
 static void fill_train_args(TrainArgs &A, HostModel &hm, const float4 *data, uint32_t n_data, uint32_t batch, float over_weight) {
@@ -433,6 +559,9 @@ static void fill_train_args(TrainArgs &A, HostModel &hm, const float4 *data, uin
     for (int l = 0; l < 4; ++l) { A.gdz[l] = p; p += rows * kHid; }
     A.grad = hm.grad;
     A.loss = hm.loss;
+    A.w_part = hm.part;
+    A.out_part = hm.part + size_t(kHidden) * wgrad_chunks(hm.rows_cap) * kTcRows * kHid;
+    A.fail = reinterpret_cast<uint32_t *>(A.out_part + size_t(hm.rows_cap / 32u) * kOutPart);
 }
 
 static void set_attributes() {
@@ -441,6 +570,7 @@ static void set_attributes() {
     cudaFuncSetAttribute(train_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(train_smem_bytes()));
     cudaFuncSetAttribute(predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(forward_smem_bytes()));
     cudaFuncSetAttribute(predict_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc_smem_bytes()));
+    cudaFuncSetAttribute(wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(wgrad_smem_bytes()));
     done = true;
 }
 
@@ -449,10 +579,17 @@ static void launch_gradients(const TrainArgs &A, cudaStream_t st) {
     set_attributes();
     const uint32_t blocks = (A.batch + kRowsPerBlock - 1) / kRowsPerBlock;
     train_fwd_bwd_kernel<<<blocks, 32 * kWarpsTrain, train_smem_bytes(), st>>>(A);
-    const uint32_t chunks = (A.batch + kChunk - 1) / kChunk;
-    wgrad_kernel<<<dim3(chunks, 1), 128, 0, st>>>(A.gdz[0], A.gx, kInPad, A.batch, A.grad + kW0);
-    for (int l = 1; l < kHidden; ++l) wgrad_kernel<<<dim3(chunks, 1), 128, 0, st>>>(A.gdz[l], A.gh[l - 1], kHid, A.batch, A.grad + w_offset(l));
-    for (int l = 0; l < kHidden; ++l) bias_grad_kernel<<<64, 256, 0, st>>>(A.gdz[l], A.batch, A.grad + b_offset(l));
+    WgradArgs G;
+    G.h[0] = A.gx;
+    for (int l = 1; l < kHidden; ++l) G.h[l] = A.gh[l - 1];
+    for (int l = 0; l < kHidden; ++l) G.dz[l] = A.gdz[l];
+    G.batch = A.batch;
+    G.chunks = wgrad_chunks(A.batch);
+    G.part = A.w_part;
+    G.fail = A.fail;
+    wgrad_tc_kernel<<<dim3(G.chunks, kHidden), kTcRows, wgrad_smem_bytes(), st>>>(G);
+    wgrad_reduce_kernel<<<(kHidden * kTcRows * kHid + 255) / 256, 256, 0, st>>>(A.w_part, G.chunks, A.grad);
+    out_reduce_kernel<<<1, 128, 0, st>>>(A.out_part, blocks * kWarpsTrain, A.grad, A.loss);
 }
 
 static HostModel *find(uint64_t id) {
@@ -637,6 +774,7 @@ int fpt_cuda_mlp_create(const struct FptRenderConfig *config, const struct FptCu
         }
     }
     if (!check(cudaStreamSynchronize(c.stream), "training", error, error_len)) { mlp::free_model(hm); return 1; }
+    if (mc->steps > 0 && mlp::gradients_failed(*hm, c.stream, error, error_len)) { mlp::free_model(hm); return 1; }
     auto t2 = std::chrono::steady_clock::now();
     const uint64_t id = mlp::g_next_model++;
     mlp::models()[id] = hm;
@@ -777,7 +915,8 @@ int fpt_cuda_mlp_gradients(uint64_t model, const float *points_xyzw, size_t n, f
          check(cudaMemcpyAsync(gradients, hm->grad, mlp::kParams * 4, cudaMemcpyDeviceToHost, c.stream), "gradient readback", error, error_len) &&
          check(cudaMemcpyAsync(&l, hm->loss, 4, cudaMemcpyDeviceToHost, c.stream), "loss readback", error, error_len) &&
          check(cudaMemsetAsync(hm->grad, 0, mlp::kParams * 4, c.stream), "grad reset", error, error_len) &&
-         check(cudaStreamSynchronize(c.stream), "gradient pass", error, error_len);
+         check(cudaStreamSynchronize(c.stream), "gradient pass", error, error_len) &&
+         !mlp::gradients_failed(*hm, c.stream, error, error_len);
     if (loss) *loss = l / float(n);
     return ok ? 0 : 1;
 }

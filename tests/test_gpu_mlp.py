@@ -109,6 +109,36 @@ def test_gradients_match_oracle(blank_model):
     assert np.abs(pad).max() < 1e-3 * np.abs(g[:7168]).max()   # padding columns carry no real gradient
 
 
+def test_gradients_are_deterministic(blank_model):
+    """The weight and bias gradients come from tcgen05 MMAs per 512-row chunk and a reduction in chunk order, the
+    output layer and the loss from per-warp sums added in warp order: no floating-point atomics, so the same batch
+    gives the same bits (here 20000 rows: 40 chunks, the last one ragged)."""
+    params = scenes.random_mlp_params(13)
+    nx.mlp_set_params(blank_model, params)
+    pts = _points(20000, 8)
+    g1, l1 = nx.mlp_gradients(blank_model, pts, 10.0)
+    g2, l2 = nx.mlp_gradients(blank_model, pts, 10.0)
+    assert np.array_equal(g1, g2) and l1 == l2
+    g_ref, _ = oracle.mlp_gradients(params, *BULB_BOX, pts, 10.0, emulate_bf16=True)
+    assert np.linalg.norm(g1 - g_ref) <= 2e-2 * np.linalg.norm(g_ref)
+
+
+def test_training_is_deterministic(native):
+    """Two trainings from the same seed on uniformly sampled points end with the same parameters, bit for bit.
+    (Near-surface points are appended by warp-aggregated atomics, so the sample set of a run with near_fraction > 0
+    can differ in the points kept from the last rejection round.)"""
+    cfg, ext = scenes.mandelbulb_primary(8, 8)
+    mc = nx.mlp_config(*BULB_BOX, points=1 << 18, near_fraction=0.0, steps=60, batch=4096, lr=2e-3, seed=5)
+    params = []
+    for _ in range(2):
+        h, _ = nx.mlp_create(cfg, ext, mc)
+        try:
+            params.append(nx.mlp_get_params(h))
+        finally:
+            nx.mlp_destroy(h)
+    assert np.array_equal(params[0], params[1])
+
+
 @pytest.fixture(scope="module")
 def trained_bulb(native):
     cfg, ext = scenes.mandelbulb_primary(8, 8)
