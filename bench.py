@@ -183,12 +183,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
-    ap.add_argument("--only", default="", choices=["", "plain", "box", "skip", "voxel"],
+    ap.add_argument("--only", default="", choices=["", "plain", "box", "skip", "voxel", "train"],
                     help="render only this march (profiling runs: no training unless skip, no JSON contract line)")
     ap.add_argument("--res", default=f"{W}x{H}", help="--only runs: image size WxH")
     ap.add_argument("--spp", type=int, default=SPP, help="--only runs: samples per pixel")
     ap.add_argument("--engine", default="tcgen05", choices=["tcgen05", "mma_sync"],
                     help="surrogate network engine of the skip arm")
+    ap.add_argument("--voxel-res", type=int, default=1024, help="--only voxel: grid resolution")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
@@ -494,8 +495,16 @@ def run_only(args):
     build.build()
     nx.set_network_engine(nx.NET_TCGEN05 if args.engine == "tcgen05" else nx.NET_MMA_SYNC)
     w, h = (int(v) for v in args.res.lower().split("x"))
-    if args.only == "voxel":   # 1024^3 Mandelbox occupancy bricks, primary + shadow DDA
-        cfg, ext = scenes.voxel_mandelbox(1024, w, h)
+    if args.only == "train":   # the surrogate's training recipe, `steps` x 10 Adam steps
+        b = scenes.mandelbulb_path(64, 64, 1)
+        mc = surrogate_config()
+        mc.steps = args.steps * 10
+        model, st = nx.mlp_create(b.cfg, b.ext, mc)
+        nx.mlp_destroy(model)
+        print(json.dumps({"only": "train", "steps": mc.steps, "train_ms": st["train_ms"], "loss_last": st["loss_last"]}), flush=True)
+        return
+    if args.only == "voxel":   # Mandelbox occupancy bricks (1024^3 by default), primary + shadow DDA
+        cfg, ext = scenes.voxel_mandelbox(args.voxel_res, w, h)
         info = nx.voxel_build(cfg, ext, 8)
         for _ in range(args.warmup):
             nx.voxel_render(cfg, ext, image=False)
