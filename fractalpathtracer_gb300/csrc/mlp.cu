@@ -197,15 +197,218 @@ __global__ void __launch_bounds__(32 * kWarpsTrain, 2) train_fwd_bwd_kernel(Trai
     }
 }
 
+// ---------------------------------------------------------------- forward + backward on tcgen05
+// The training pass of train_fwd_bwd_kernel with its products on the
+// 5th-generation tensor cores: 128 rows per CTA, one row per thread, the
+// M = 128, N = 64, K = 16 MMA shape of the inference pass.  Forward: per
+// layer H_l x W_l^T into a 128 x 64 FP32 accumulator in tensor memory; each
+// thread reads its row, adds the bias, stores Z_l (bf16) and H_{l+1} =
+// SiLU(Z_l) (bf16) to global memory and into the next layer's operand tile.
+// Backward: dZ_4 = dout W4 o SiLU'(Z_4) per row, then dZ_l = (dZ_{l+1} W_l) o
+// SiLU'(Z_l) with B = W_l^T staged at set-up.  Same arithmetic as the
+// mma.sync pass (BF16 operands, FP32 accumulation, SiLU and its derivative on
+// the FP32 pre-activation / its bf16 copy); only the order of the FP32 sums
+// differs.
+// Two floats as a packed pair of bf16 (lo in the low half).
+__device__ __forceinline__ uint32_t bf16_pair(float lo, float hi) {
+    return uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(lo))) | (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(hi))) << 16);
+}
+
+struct TrainTcSmem {
+    alignas(128) unsigned char act[kTcRows * kInPad * 2];        // operand A: features, activations, then deltas
+    alignas(128) unsigned char w0[kHid * kInPad * 2];            // forward B of layer 0: W0[n][k]
+    alignas(128) unsigned char w[kHidden - 1][kHid * kHid * 2];  // forward B: W_l[n][k]
+    alignas(128) unsigned char wt[kHidden - 1][kHid * kHid * 2]; // backward B: W_l^T, element (k, n) = W_l[n][k]
+    float b[kHidden][kHid];
+    float w4[kHid];
+    float b4;
+    uint32_t tmem;
+    alignas(8) uint64_t bar;
+    unsigned char slack[4096];
+};
+inline size_t train_tc_smem_bytes() { return sizeof(TrainTcSmem); }
+
+// One round of MMAs (A = the act tile with K = k columns, B at `b`) into the
+// accumulator; every thread then holds its row in r.  False when the MMAs did
+// not complete within kMmaWaitNs (the same in every thread).
+__device__ __forceinline__ bool train_round(TrainTcSmem &sm, uint32_t b, int k, uint32_t &phase, uint32_t r[64]) {
+    const int t = threadIdx.x;
+    const uint32_t act = umma::smem_u32(sm.act);
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {
+        umma::fence_after_sync();
+        for (int j = 0; j < k / 16; ++j)
+            umma::mma_bf16(sm.tmem, umma::smem_desc(act + uint32_t(j) * 2u * kActK, kActK, kCore),
+                           umma::smem_desc(b + uint32_t(j) * 2u * kWK, kWK, kCore), kTcIdesc, uint32_t(j));
+        umma::mma_commit(&sm.bar);
+    }
+    const int late = t == 0 ? int(!umma::mbar_wait(&sm.bar, phase, kMmaWaitNs)) : 0;
+    phase ^= 1u;
+    if (__syncthreads_or(late)) return false;
+    umma::fence_after_sync();
+    __syncwarp();
+    umma::tmem_ld64(sm.tmem + (uint32_t(t & ~31) << 16), r);
+    return true;
+}
+
+__device__ __forceinline__ void store_row64(__nv_bfloat16 *g, const uint32_t h[32]) {
+    uint4 *d = reinterpret_cast<uint4 *>(g);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) d[q] = make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+}
+
+__global__ void __launch_bounds__(kTcRows) train_fwd_bwd_tc_kernel(TrainArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TrainTcSmem &sm = *reinterpret_cast<TrainTcSmem *>(smem_raw);
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const Model &M = A.model;
+    if (__syncthreads_or(t == 0 && *reinterpret_cast<volatile uint32_t *>(A.fail) != 0u)) return;   // an earlier launch timed out
+    for (int i = t; i < kHid * kInPad; i += kTcRows) {
+        const int n = i / kInPad, k = i - n * kInPad;
+        *reinterpret_cast<__nv_bfloat16 *>(sm.w0 + w_core_offset(n, k)) = M.wbf[kW0 + i];
+    }
+    for (int l = 1; l < kHidden; ++l)
+        for (int i = t; i < kHid * kHid; i += kTcRows) {
+            const int n = i / kHid, k = i - n * kHid;
+            *reinterpret_cast<__nv_bfloat16 *>(sm.w[l - 1] + w_core_offset(n, k)) = M.wbf[w_offset(l) + i];
+            *reinterpret_cast<__nv_bfloat16 *>(sm.wt[l - 1] + w_core_offset(k, n)) = M.wbf[w_offset(l) + i];
+        }
+    for (int i = t; i < kHidden * kHid; i += kTcRows) sm.b[i / kHid][i % kHid] = M.params[b_offset(i / kHid) + i % kHid];
+    for (int i = t; i < kHid; i += kTcRows) sm.w4[i] = __bfloat162float(M.wbf[kW4 + i]);
+    if (t == 0) {
+        sm.b4 = M.params[kB4];
+        umma::mbar_init(&sm.bar, 1u);
+    }
+    if (t < 32) {
+        __syncwarp();
+        umma::tmem_alloc(&sm.tmem, kTcCols);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t act = umma::smem_u32(sm.act);
+    const uint32_t row = blockIdx.x * kTcRows + uint32_t(t);
+    const bool valid = row < A.batch;
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) s = A.data[A.identity ? row : hash2(A.seed + A.step * 7919u, row) % A.n_data];
+    {
+        const float u[3] = {(s.x - M.center[0]) * M.inv_half[0], (s.y - M.center[1]) * M.inv_half[1], (s.z - M.center[2]) * M.inv_half[2]};
+        uint32_t f[kInPad / 2];
+        feature_pairs(u, f);
+#pragma unroll
+        for (int kc = 0; kc < kInPad / 8; ++kc) umma::st_shared_v4(act + act_offset(t, kc), f[4 * kc], f[4 * kc + 1], f[4 * kc + 2], f[4 * kc + 3]);
+        uint4 *gx = reinterpret_cast<uint4 *>(A.gx + size_t(row) * kInPad);
+#pragma unroll
+        for (int q = 0; q < kInPad / 8; ++q) gx[q] = make_uint4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+    }
+    uint32_t phase = 0, r[64], h[32];
+    bool ok = true;
+    float dout = 0.0f, loss = 0.0f;
+    // forward
+    for (int L = 0; L < kHidden && ok; ++L) {
+        ok = train_round(sm, umma::smem_u32(L == 0 ? sm.w0 : sm.w[L - 1]), L == 0 ? kInPad : kHid, phase, r);
+        if (!ok) break;
+        uint32_t z[32];
+#pragma unroll
+        for (int c = 0; c < kHid; c += 2) {
+            const float z0 = __uint_as_float(r[c]) + sm.b[L][c], z1 = __uint_as_float(r[c + 1]) + sm.b[L][c + 1];
+            z[c >> 1] = bf16_pair(z0, z1);
+            h[c >> 1] = bf16_pair(silu(z0), silu(z1));
+        }
+        store_row64(A.gz[L] + size_t(row) * kHid, z);
+        if (L + 1 < kHidden) {
+            store_row64(A.gh[L] + size_t(row) * kHid, h);
+#pragma unroll
+            for (int kc = 0; kc < kHid / 8; ++kc) umma::st_shared_v4(act + act_offset(t, kc), h[4 * kc], h[4 * kc + 1], h[4 * kc + 2], h[4 * kc + 3]);
+        }
+    }
+    if (ok) {
+        // output layer, loss, dZ4 (h holds H4, r + bias the FP32 Z4)
+        float out = sm.b4;
+#pragma unroll
+        for (int c = 0; c < kHid; c += 2) {
+            out += __uint_as_float(h[c >> 1] << 16) * sm.w4[c];
+            out += __uint_as_float(h[c >> 1] & 0xffff0000u) * sm.w4[c + 1];
+        }
+        const float y = s.w * A.inv_label_scale;
+        const float e = out - y;
+        const float wgt = e > 0.0f ? A.over_weight : 1.0f;
+        dout = valid ? 2.0f * wgt * e / float(A.batch) : 0.0f;
+        loss = valid ? wgt * e * e : 0.0f;
+        float *part = A.out_part + size_t(blockIdx.x * (kTcRows / 32) + warp) * kOutPart;
+        for (int c = 0; c < kHid; ++c) {
+            const uint32_t hb = (c & 1) ? (h[c >> 1] & 0xffff0000u) : (h[c >> 1] << 16);
+            float v = dout * __uint_as_float(hb);
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) part[c] = v;
+        }
+        {
+            float v = dout, lv = loss;
+            for (int o = 16; o > 0; o >>= 1) {
+                v += __shfl_xor_sync(0xffffffffu, v, o);
+                lv += __shfl_xor_sync(0xffffffffu, lv, o);
+            }
+            if (lane == 0) {
+                part[kHid] = v;
+                part[kHid + 1] = lv;
+            }
+        }
+        uint32_t d[32];
+#pragma unroll
+        for (int c = 0; c < kHid; c += 2) {
+            const float z0 = __bfloat162float(__float2bfloat16_rn(__uint_as_float(r[c]) + sm.b[3][c]));
+            const float z1 = __bfloat162float(__float2bfloat16_rn(__uint_as_float(r[c + 1]) + sm.b[3][c + 1]));
+            d[c >> 1] = bf16_pair(dout * sm.w4[c] * silu_grad(z0), dout * sm.w4[c + 1] * silu_grad(z1));
+        }
+        store_row64(A.gdz[3] + size_t(row) * kHid, d);
+#pragma unroll
+        for (int kc = 0; kc < kHid / 8; ++kc) umma::st_shared_v4(act + act_offset(t, kc), d[4 * kc], d[4 * kc + 1], d[4 * kc + 2], d[4 * kc + 3]);
+    }
+    // backward through hidden layers 3, 2, 1: dZ_l = (dZ_{l+1} W_l) o SiLU'(Z_l)
+    for (int l = kHidden - 1; l >= 1 && ok; --l) {
+        ok = train_round(sm, umma::smem_u32(sm.wt[l - 1]), kHid, phase, r);
+        if (!ok) break;
+        const uint4 *zg = reinterpret_cast<const uint4 *>(A.gz[l - 1] + size_t(row) * kHid);
+        uint32_t d[32];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint4 zz = zg[q];
+            const uint32_t zw[4] = {zz.x, zz.y, zz.z, zz.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = q * 8 + e * 2;
+                const float z0 = __uint_as_float(zw[e] << 16), z1 = __uint_as_float(zw[e] & 0xffff0000u);
+                d[c >> 1] = bf16_pair(__uint_as_float(r[c]) * silu_grad(z0), __uint_as_float(r[c + 1]) * silu_grad(z1));
+            }
+        }
+        store_row64(A.gdz[l - 1] + size_t(row) * kHid, d);
+        if (l > 1) {
+#pragma unroll
+            for (int kc = 0; kc < kHid / 8; ++kc) umma::st_shared_v4(act + act_offset(t, kc), d[4 * kc], d[4 * kc + 1], d[4 * kc + 2], d[4 * kc + 3]);
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (t < 32) {
+        __syncwarp();
+        umma::fence_after_sync();
+        umma::tmem_dealloc(sm.tmem, kTcCols);
+    }
+    if (!ok && t == 0) atomicOr(A.fail, 2u);
+}
+
 // ---------------------------------------------------------------- weight gradients on tcgen05
-// For layer l and a chunk of the batch: D[m][n] = sum_b H_l[b][m] dZ_l[b][n]
+// For layer l and a 256-row chunk of the batch: D[m][n] = sum_b H_l[b][m] dZ_l[b][n]
 // (m < K_l: dW_l[n][m]; m = K_l: a row of ones in H^T, so D[K_l][n] is the
 // bias gradient db_l[n]).  A = H^T (128 x 64-row tile of the batch, K-major),
 // B = dZ^T (64 x 64), the M = 128, N = 64, K = 16 MMA shape of the forward
 // pass, accumulated over the chunk in one 64-column tensor-memory tile.  Each
 // CTA writes its 128 x 64 partial; wgrad_reduce_kernel adds the chunks in
 // order (no atomics: the same data gives the same bits).
-constexpr uint32_t kWgChunk = 512;            // batch rows per CTA
+constexpr uint32_t kWgChunk = 256;            // batch rows per CTA
 constexpr uint32_t kWgTile = 64;              // batch rows per round of 4 MMAs
 struct WgSmem {
     alignas(128) unsigned char a[kTcRows * kWgTile * 2];   // H^T tile, [k chunk][m group][8 m][8 k]
@@ -224,8 +427,53 @@ struct WgradArgs {
     uint32_t *fail;                      // set (bit 2) when an MMA does not complete in time; later launches skip their work
 };
 
-__device__ __forceinline__ uint32_t bf16_pair(float lo, float hi) {
-    return uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(lo))) | (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(hi))) << 16);
+// Global tile loads of one round (64 batch rows): H rows as 16-byte vectors
+// (8 columns each, at most 7 per thread) and dZ rows (4 per thread).
+struct WgLoad {
+    uint4 h[(kTcRows * kWgTile / 8 + kTcRows - 1) / kTcRows];
+    uint4 dz[kHid * kWgTile / 8 / kTcRows];
+};
+__device__ __forceinline__ void wg_load(WgLoad &L, const __nv_bfloat16 *H, const __nv_bfloat16 *DZ, int kcols, uint32_t kb, uint32_t b1) {
+    const int t = threadIdx.x, nvec = kcols / 8;
+#pragma unroll
+    for (int q = 0; q < int(sizeof(L.h) / sizeof(uint4)); ++q) {
+        const int i = t + q * kTcRows, row = i / nvec, v = i - row * nvec;
+        L.h[q] = (row < int(kWgTile) && kb + uint32_t(row) < b1)
+                     ? *reinterpret_cast<const uint4 *>(H + size_t(kb + row) * kcols + v * 8)
+                     : make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int q = 0; q < int(sizeof(L.dz) / sizeof(uint4)); ++q) {
+        const int i = t + q * kTcRows, row = i >> 3, v = i & 7;
+        L.dz[q] = kb + uint32_t(row) < b1 ? *reinterpret_cast<const uint4 *>(DZ + size_t(kb + row) * kHid + v * 8)
+                                          : make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+// The loaded vectors into the K-major operand tiles (a transpose: each of a
+// vector's 8 values goes to its own row of H^T / dZ^T), and the row of ones.
+__device__ __forceinline__ void wg_store(const WgLoad &L, WgSmem &sm, int kcols, uint32_t kb, uint32_t b1) {
+    const int t = threadIdx.x, nvec = kcols / 8;
+#pragma unroll
+    for (int q = 0; q < int(sizeof(L.h) / sizeof(uint4)); ++q) {
+        const int i = t + q * kTcRows, row = i / nvec, v = i - row * nvec;
+        if (row >= int(kWgTile)) continue;
+        const uint32_t w[4] = {L.h[q].x, L.h[q].y, L.h[q].z, L.h[q].w};
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int m = v * 8 + e;
+            *reinterpret_cast<uint16_t *>(sm.a + act_offset(m, row >> 3) + (row & 7) * 2) = uint16_t(w[e >> 1] >> ((e & 1) * 16));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < int(sizeof(L.dz) / sizeof(uint4)); ++q) {
+        const int i = t + q * kTcRows, row = i >> 3, v = i & 7;
+        const uint32_t w[4] = {L.dz[q].x, L.dz[q].y, L.dz[q].z, L.dz[q].w};
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            *reinterpret_cast<uint16_t *>(sm.b + w_core_offset(v * 8 + e, row)) = uint16_t(w[e >> 1] >> ((e & 1) * 16));
+    }
+    if (t < int(kWgTile))   // H^T row kcols: ones on the chunk's rows, so its product with dZ is the bias gradient
+        *reinterpret_cast<uint16_t *>(sm.a + act_offset(kcols, t >> 3) + (t & 7) * 2) = kb + uint32_t(t) < b1 ? 0x3F80u : 0u;
 }
 
 __global__ void __launch_bounds__(kTcRows) wgrad_tc_kernel(WgradArgs G) {
@@ -247,6 +495,11 @@ __global__ void __launch_bounds__(kTcRows) wgrad_tc_kernel(WgradArgs G) {
         umma::tmem_alloc(&sm.tmem, kTcCols);
         umma::tmem_relinquish();
     }
+    // H^T rows above the ones row stay zero for every round
+    for (int i = t; i < (kTcRows - kcols - 1) * int(kWgTile); i += kTcRows) {
+        const int m = kcols + 1 + i / int(kWgTile), k = i % int(kWgTile);
+        *reinterpret_cast<uint16_t *>(sm.a + act_offset(m, k >> 3) + (k & 7) * 2) = 0u;
+    }
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
@@ -254,39 +507,10 @@ __global__ void __launch_bounds__(kTcRows) wgrad_tc_kernel(WgradArgs G) {
     const uint32_t b0 = blockIdx.x * kWgChunk, b1 = min(G.batch, b0 + kWgChunk);
     uint32_t phase = 0;
     bool fail = false, any = false;
+    WgLoad L;
+    wg_load(L, H, DZ, kcols, b0, b1);
     for (uint32_t kb = b0; kb < b1; kb += kWgTile) {   // the same trips in every thread
-        // A: thread t holds column m = t of H^T (row t of the tile), 8 batch rows per 16-byte store
-#pragma unroll 1
-        for (int kc = 0; kc < int(kWgTile / 8); ++kc) {
-            uint32_t w[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                float v[2];
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const uint32_t r = kb + uint32_t(kc * 8 + q * 2 + e);
-                    v[e] = r >= b1 ? 0.0f : (t < kcols ? __bfloat162float(H[size_t(r) * kcols + t]) : (t == kcols ? 1.0f : 0.0f));
-                }
-                w[q] = bf16_pair(v[0], v[1]);
-            }
-            umma::st_shared_v4(a + act_offset(t, kc), w[0], w[1], w[2], w[3]);
-        }
-        // B: thread t holds neuron n = t % 64 for half of the tile's batch rows
-        {
-            const int n = t & (kHid - 1), kc0 = (t >> 6) * int(kWgTile / 16);
-#pragma unroll 1
-            for (int kc = kc0; kc < kc0 + int(kWgTile / 16); ++kc) {
-                uint32_t w[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t r = kb + uint32_t(kc * 8 + q * 2);
-                    const float v0 = r < b1 ? __bfloat162float(DZ[size_t(r) * kHid + n]) : 0.0f;
-                    const float v1 = r + 1 < b1 ? __bfloat162float(DZ[size_t(r + 1) * kHid + n]) : 0.0f;
-                    w[q] = bf16_pair(v0, v1);
-                }
-                umma::st_shared_v4(bt + w_core_offset(n, kc * 8), w[0], w[1], w[2], w[3]);
-            }
-        }
+        wg_store(L, sm, kcols, kb, b1);
         umma::fence_smem_to_async();
         umma::fence_before_sync();
         __syncthreads();
@@ -298,6 +522,7 @@ __global__ void __launch_bounds__(kTcRows) wgrad_tc_kernel(WgradArgs G) {
                                kTcIdesc, (any || j > 0u) ? 1u : 0u);
             umma::mma_commit(&sm.bar);
         }
+        if (kb + kWgTile < b1) wg_load(L, H, DZ, kcols, kb + kWgTile, b1);   // the next round's loads overlap the MMAs
         const int late = t == 0 ? int(!umma::mbar_wait(&sm.bar, phase, kMmaWaitNs)) : 0;
         phase ^= 1u;
         any = true;
@@ -341,15 +566,24 @@ __global__ void __launch_bounds__(256) wgrad_reduce_kernel(const float *part, ui
     else grad[b_offset(layer) + n] += s;
 }
 
-// Output layer and loss: grad[W4], grad[b4] and the loss += the warps' partial sums, added in warp order.
-__global__ void __launch_bounds__(128) out_reduce_kernel(const float *part, uint32_t warps, float *grad, float *loss) {
-    const uint32_t j = threadIdx.x;
-    if (j >= kOutPart) return;
+// Output layer and loss: grad[W4], grad[b4] and the loss += the warps' partial
+// sums.  Thread (j, g) adds warps g, g + 8, ... in order; thread (j, 0) then
+// adds the 8 group sums in order (a fixed order: the same bits every run).
+constexpr int kOutGroups = 8;
+__global__ void __launch_bounds__(kOutPart * kOutGroups) out_reduce_kernel(const float *part, uint32_t warps, float *grad, float *loss) {
+    __shared__ float sums[kOutGroups][kOutPart];
+    const uint32_t j = threadIdx.x % kOutPart, g = threadIdx.x / kOutPart;
     float s = 0.0f;
-    for (uint32_t w = 0; w < warps; ++w) s += part[size_t(w) * kOutPart + j];
-    if (j < uint32_t(kHid)) grad[kW4 + j] += s;
-    else if (j == uint32_t(kHid)) grad[kB4] += s;
-    else *loss += s;
+    for (uint32_t w = g; w < warps; w += kOutGroups) s += part[size_t(w) * kOutPart + j];
+    sums[g][j] = s;
+    __syncthreads();
+    if (g != 0u) return;
+    float total = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kOutGroups; ++k) total += sums[k][j];
+    if (j < uint32_t(kHid)) grad[kW4 + j] += total;
+    else if (j == uint32_t(kHid)) grad[kB4] += total;
+    else *loss += total;
 }
 
 __global__ void __launch_bounds__(256) adam_kernel(float *params, float *m, float *v, float *grad, __nv_bfloat16 *wbf, float lr,
@@ -571,6 +805,7 @@ static void set_attributes() {
     cudaFuncSetAttribute(predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(forward_smem_bytes()));
     cudaFuncSetAttribute(predict_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc_smem_bytes()));
     cudaFuncSetAttribute(wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(wgrad_smem_bytes()));
+    cudaFuncSetAttribute(train_fwd_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(train_tc_smem_bytes()));
     done = true;
 }
 
@@ -578,7 +813,9 @@ static void set_attributes() {
 static void launch_gradients(const TrainArgs &A, cudaStream_t st) {
     set_attributes();
     const uint32_t blocks = (A.batch + kRowsPerBlock - 1) / kRowsPerBlock;
-    train_fwd_bwd_kernel<<<blocks, 32 * kWarpsTrain, train_smem_bytes(), st>>>(A);
+    // forward + backward on the network engine of the inference passes (tcgen05 by default)
+    if (ctx().network_engine == FPT_CUDA_NET_MMA_SYNC) train_fwd_bwd_kernel<<<blocks, 32 * kWarpsTrain, train_smem_bytes(), st>>>(A);
+    else train_fwd_bwd_tc_kernel<<<blocks, kTcRows, train_tc_smem_bytes(), st>>>(A);
     WgradArgs G;
     G.h[0] = A.gx;
     for (int l = 1; l < kHidden; ++l) G.h[l] = A.gh[l - 1];
@@ -589,7 +826,7 @@ static void launch_gradients(const TrainArgs &A, cudaStream_t st) {
     G.fail = A.fail;
     wgrad_tc_kernel<<<dim3(G.chunks, kHidden), kTcRows, wgrad_smem_bytes(), st>>>(G);
     wgrad_reduce_kernel<<<(kHidden * kTcRows * kHid + 255) / 256, 256, 0, st>>>(A.w_part, G.chunks, A.grad);
-    out_reduce_kernel<<<1, 128, 0, st>>>(A.out_part, blocks * kWarpsTrain, A.grad, A.loss);
+    out_reduce_kernel<<<1, kOutPart * kOutGroups, 0, st>>>(A.out_part, blocks * kWarpsTrain, A.grad, A.loss);
 }
 
 static HostModel *find(uint64_t id) {

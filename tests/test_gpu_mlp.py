@@ -91,7 +91,10 @@ def test_engines_agree(blank_model):
     assert d.max() <= 1e-2 * scale
 
 
-def test_gradients_match_oracle(blank_model):
+@pytest.mark.parametrize("engine", ENGINES, indirect=True)
+def test_gradients_match_oracle(blank_model, engine):
+    """Gradients and loss of one pass against the FP64 oracle, with the training's forward/backward on either
+    engine (tcgen05 by default, mma.sync); the weight gradients run on tcgen05 in both."""
     params = scenes.random_mlp_params(12)
     nx.mlp_set_params(blank_model, params)
     pts = _points(1000, 6)   # not a multiple of the 128-row block: exercises the ragged tail
