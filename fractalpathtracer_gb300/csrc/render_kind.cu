@@ -93,7 +93,8 @@ static cudaError_t launch_path_impl(const PathLaunch &pl, cudaStream_t stream) {
         if (t) pl.timer->end(stream);
         ++launches;
     };
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = scene_to_constant(pl.scene, stream);
+    if (e != cudaSuccess) return e;
     for (uint64_t wb = 0; wb < total; wb += cap) {
         W.wave_base = uint32_t(wb);
         W.n_paths = uint32_t(std::min<uint64_t>(cap, total - wb));
@@ -191,6 +192,7 @@ int FPT_CAT(skip_pass_blocks_k, FPT_KIND)(bool tc, int sms) {
     return sms * (per_sm > 0 ? per_sm : 1);
 }
 void FPT_CAT(launch_skip_pass_k, FPT_KIND)(const WaveParams &W, const SkipArgs &A, bool tc, int blocks, cudaStream_t stream) {
+    scene_to_constant(W.scene, stream);   // a failed copy surfaces at the launch check after the pass
     if (tc)
         skip_march_tc_kernel<FPT_KIND><<<blocks, mlp::kTcRows, mlp::tc_smem_bytes(), stream>>>(W, A);
     else

@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_march_kernel(WavePara
     mlp::SmemWeights &sw = *reinterpret_cast<mlp::SmemWeights *>(smem_raw);
     mlp::WarpForward *wf_all =
         reinterpret_cast<mlp::WarpForward *>(smem_raw + ((sizeof(mlp::SmemWeights) + 127) & ~size_t(127)));
-    const DeviceScene &S = *W.scene;
+    const DeviceScene &S = c_scene;
     const uint32_t total = W.counters[C_SKIPN];
     if (total == 0u) return;
     mlp::load_weights(sw, A.M);
@@ -358,7 +358,7 @@ template <int KIND>
 __global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WaveParams W, SkipArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
-    const DeviceScene &S = *W.scene;
+    const DeviceScene &S = c_scene;
     const uint32_t total = W.counters[C_SKIPN];
     if (total == 0u) return;
     mlp::tc_setup(sm, A.M);

@@ -99,6 +99,15 @@ __device__ __forceinline__ bool loop_guard(uint32_t &trips, unsigned long long t
     return true;
 }
 
+// The scene of a single-scene launch, copied into this translation unit's
+// constant memory before the launch (scene_to_constant): all lanes read the
+// same scene fields, which the constant cache serves as instruction operands
+// instead of one load instruction per field and lane.
+static __constant__ DeviceScene c_scene;
+static inline cudaError_t scene_to_constant(const DeviceScene *scene, cudaStream_t st) {
+    return cudaMemcpyToSymbolAsync(c_scene, scene, sizeof(DeviceScene), 0, cudaMemcpyDeviceToDevice, st);
+}
+
 struct WaveParams {
     const DeviceScene *scene;
     PathRec *paths;
@@ -237,7 +246,7 @@ __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
         bool in_wave = p < W.n_paths;
         uint32_t px = 0, py = 0, s_rel = 0, k = 0;
         bool valid = false;
-        const DeviceScene *sp = W.scene;
+        const DeviceScene *sp = BATCH ? W.scene : &c_scene;
         if (in_wave) {
             if (BATCH) {
                 const uint32_t g = W.wave_base + p;
@@ -329,7 +338,7 @@ struct MarchJob {
 // in FP64 (march_fp64), which decides hit or miss and the hit distance.
 template <int KIND, bool BATCH = false, int BLOCK = 128, int MINB = 7, bool FP64 = false>
 __global__ void __launch_bounds__(BLOCK, MINB) march_kernel(WaveParams W, int cur) {
-    const DeviceScene *sp = W.scene;   // the lane's scene (per job when BATCH)
+    const DeviceScene *sp = BATCH ? W.scene : &c_scene;   // the lane's scene (per job when BATCH)
     const uint32_t n_path = W.counters[C_MARCH0 + cur];
     const uint32_t total = n_path + W.counters[C_SHADOW0 + cur];
     const uint32_t *qm = W.q_march[cur];
@@ -595,7 +604,7 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
             path = W.q_shade[i];
             PathRec R = W.paths[path];
             uint32_t state = fbits(R.color.w);
-            const DeviceScene &S = BATCH ? W.scenes[state >> 16] : *W.scene;
+            const DeviceScene &S = BATCH ? W.scenes[state >> 16] : c_scene;
             const bool ggx = S.brdf == FPT_CUDA_BRDF_LAMBERT_GGX;
             const int bounce = int(state & 0xffu);
             const uint32_t slot = fbits(R.light.w);
@@ -837,7 +846,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(WaveParams W) {
     const PathRec &R = W.paths[p];
     uint32_t state = fbits(R.color.w);
     if (!(state & PF_VALID)) return;
-    const DeviceScene &S = BATCH ? W.scenes[state >> 16] : *W.scene;
+    const DeviceScene &S = BATCH ? W.scenes[state >> 16] : c_scene;
     float3 col = mk3(0.0f);
     if (!(state & PF_INVISIBLE)) {
         float3 light = mk3(R.light.x + R.shadow.x, R.light.y + R.shadow.y, R.light.z + R.shadow.z);
