@@ -44,7 +44,7 @@ struct PathLaunch {
     uint32_t width, height;
     uint32_t bounces;
     float4 *accum;              // width*height, running mean
-    float4 *sample_rgb;         // width*height*(sample_end-sample_begin) scratch: one colour per path
+    float4 *sample_rgb;         // (sample_end-sample_begin)*width*height scratch: one colour per path, sample-major
     void *wave_scratch;         // wave_scratch_bytes(wave_paths) bytes
     uint32_t wave_paths;        // paths per wave ("wavefront length")
     unsigned int *counters;     // 8 device words

@@ -21,9 +21,8 @@ static __global__ void __launch_bounds__(256) reduce_samples_kernel(const float4
     if (p >= pixels) return;
     float3 mean = mk3(0.0f);
     if (sample_begin > 0u) { float4 a = accum[p]; mean = mk3(a.x, a.y, a.z); }
-    const float4 *src = sample_rgb + size_t(p) * sample_count;
-    for (uint32_t i = 0; i < sample_count; ++i) {
-        float4 c = src[i];
+    for (uint32_t i = 0; i < sample_count; ++i) {   // sample-major: sample i of every pixel, then i + 1
+        float4 c = sample_rgb[size_t(i) * pixels + p];
         mean = mix3(mean, mk3(c.x, c.y, c.z), 1.0f / float(sample_begin + i + 1u));
     }
     accum[p] = make_float4(mean.x, mean.y, mean.z, 1.0f);

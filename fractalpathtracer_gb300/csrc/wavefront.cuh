@@ -46,6 +46,7 @@ struct alignas(16) PathRec {
     float4 shadow;  // xyz sun light from shadow rays, w plain-march steps a camera ray took before the march kernel
     float4 grad;    // xyz background gradient colour of the camera ray, w exact distance (PF_KNOWN_D)
 };
+static_assert(sizeof(PathRec) == 96, "path records are six float4");
 
 // A camera ray that enters the surrogate's box, queued by the camera kernel
 // for the skip pass.
@@ -187,6 +188,38 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
     return base + __popc(bal & ((1u << lane) - 1u));
 }
 
+// Appends the lanes of a whole block that want a slot in either of two
+// queues, with one atomic per queue and block (the camera kernel appends
+// every path of the wave; one atomic per warp on one counter serialised
+// over a million warps).  Every thread of the block calls it.
+constexpr uint32_t kCameraBlock = 256;
+__device__ __forceinline__ void block_append2(uint32_t *counter0, bool want0, uint32_t &slot0, uint32_t *counter1, bool want1,
+                                              uint32_t &slot1) {
+    constexpr uint32_t kWarps = kCameraBlock / 32u;
+    __shared__ uint32_t s_off[2][kWarps + 1];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const unsigned b0 = __ballot_sync(0xffffffffu, want0), b1 = __ballot_sync(0xffffffffu, want1);
+    if (lane == 0) {
+        s_off[0][warp] = uint32_t(__popc(b0));
+        s_off[1][warp] = uint32_t(__popc(b1));
+    }
+    __syncthreads();
+    if (threadIdx.x < 2u) {   // thread q: exclusive offsets of the warps, then the block's base in queue q
+        uint32_t sum = 0;
+        for (uint32_t w = 0; w < kWarps; ++w) {
+            const uint32_t c = s_off[threadIdx.x][w];
+            s_off[threadIdx.x][w] = sum;
+            sum += c;
+        }
+        s_off[threadIdx.x][kWarps] = sum ? atomicAdd(threadIdx.x == 0 ? counter0 : counter1, sum) : 0u;
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1u;
+    slot0 = s_off[0][kWarps] + s_off[0][warp] + uint32_t(__popc(b0 & below));
+    slot1 = s_off[1][kWarps] + s_off[1][warp] + uint32_t(__popc(b1 & below));
+    __syncthreads();   // s_off is reused by the next call
+}
+
 __device__ __forceinline__ void wave_pixel(const WaveParams &W, uint32_t path, uint32_t width, uint32_t height, uint32_t &px,
                                            uint32_t &py, uint32_t &s_rel, bool &valid) {
     uint32_t g = W.wave_base + path;
@@ -241,7 +274,11 @@ __global__ void first_step_kernel(const DeviceScene *scene, uint32_t *out) {
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
+__global__ void __launch_bounds__(kCameraBlock) camera_kernel(WaveParams W) {
+    // The warp's 32 consecutive path records are assembled here and leave as
+    // 16-byte stores that cover its 3 KB of records contiguously.
+    __shared__ PathRec s_rec[kCameraBlock];
+    const uint32_t lane = threadIdx.x & 31u, wbase = threadIdx.x & ~31u;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p - threadIdx.x < W.n_paths; p += gridDim.x * blockDim.x) {
         bool in_wave = p < W.n_paths;
         uint32_t px = 0, py = 0, s_rel = 0, k = 0;
@@ -272,7 +309,8 @@ __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
             PathRng rng;
             rng.init(S.rng == FPT_CUDA_RNG_PCG, S.seed, pixel, sample, uv.x, uv.y);
             PathRec R;
-            uint32_t slot = BATCH ? W.pixel_base[k] + pixel : pixel * W.sample_count + s_rel;
+            // the path's colour slot: sample-major, so a warp's 8 x 4 tile writes whole rows of pixels
+            uint32_t slot = BATCH ? W.pixel_base[k] + pixel : s_rel * (S.width * S.height) + pixel;
             R.light = make_float4(0.f, 0.f, 0.f, bitsf(slot));
             R.shadow = make_float4(0.f, 0.f, 0.f, 0.f);
             if (!camera_ray(S, uv, rng, true, rp, dr)) {
@@ -309,13 +347,25 @@ __global__ void __launch_bounds__(256) camera_kernel(WaveParams W) {
                     }
                 }
             }
-            W.paths[p] = R;
-        } else if (in_wave) {
-            W.paths[p].color = make_float4(0.f, 0.f, 0.f, 0.f);   // not a pixel of the image
+            s_rec[threadIdx.x] = R;
+        } else {
+            PathRec R;   // not a pixel of the image (state word 0)
+            R.pos = R.dir = R.color = R.light = R.shadow = R.grad = make_float4(0.f, 0.f, 0.f, 0.f);
+            s_rec[threadIdx.x] = R;
         }
-        uint32_t at = warp_append(&W.counters[C_MARCH0], march);
+        __syncwarp();
+        {
+            const float4 *src = reinterpret_cast<const float4 *>(s_rec + wbase);
+            float4 *dst = reinterpret_cast<float4 *>(W.paths + (p - lane));
+            const uint32_t records = min(32u, W.n_paths > p - lane ? W.n_paths - (p - lane) : 0u);
+#pragma unroll
+            for (uint32_t c = lane; c < 32u * 6u; c += 32u)
+                if (c / 6u < records) dst[c] = src[c];
+        }
+        __syncwarp();
+        uint32_t at = 0, sat = 0;
+        block_append2(&W.counters[C_MARCH0], march, at, &W.counters[C_SKIPN], skip, sat);
         if (march) W.q_march[0][at] = p;
-        uint32_t sat = warp_append(&W.counters[C_SKIPN], skip);
         if (skip) {
             W.q_skip[sat].origin = make_float4(rp.x, rp.y, rp.z, bitsf(p));
             W.q_skip[sat].dir = make_float4(dr.x, dr.y, dr.z, steps0);
@@ -613,9 +663,9 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
                 pixel = slot - W.pixel_base[state >> 16];
                 sample = *W.pass;
             } else {
-                const uint32_t s_rel = slot % W.sample_count;
-                pixel = slot / W.sample_count;
-                sample = W.sample_begin + s_rel;
+                const uint32_t pixels = S.width * S.height;
+                pixel = slot % pixels;
+                sample = W.sample_begin + slot / pixels;
             }
             PathRng rng = path_rng(S, pixel, sample);
             float3 hit = mk3(R.pos.x, R.pos.y, R.pos.z), dr = mk3(R.dir.x, R.dir.y, R.dir.z);
