@@ -188,14 +188,16 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
     return base + __popc(bal & ((1u << lane) - 1u));
 }
 
-// Appends the lanes of a whole block that want a slot in either of two
-// queues, with one atomic per queue and block (the camera kernel appends
-// every path of the wave; one atomic per warp on one counter serialised
-// over a million warps).  Every thread of the block calls it.
+// Appends the lanes of a whole BLOCK-thread block that want a slot in either
+// of two queues, with one atomic per queue and block (the camera and shade
+// kernels append millions of rays per pass; one atomic per warp on one
+// counter serialises over a million warps).  Every thread of the block calls
+// it.
 constexpr uint32_t kCameraBlock = 256;
+template <uint32_t BLOCK>
 __device__ __forceinline__ void block_append2(uint32_t *counter0, bool want0, uint32_t &slot0, uint32_t *counter1, bool want1,
                                               uint32_t &slot1) {
-    constexpr uint32_t kWarps = kCameraBlock / 32u;
+    constexpr uint32_t kWarps = BLOCK / 32u;
     __shared__ uint32_t s_off[2][kWarps + 1];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const unsigned b0 = __ballot_sync(0xffffffffu, want0), b1 = __ballot_sync(0xffffffffu, want1);
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(kCameraBlock) camera_kernel(WaveParams W) {
         }
         __syncwarp();
         uint32_t at = 0, sat = 0;
-        block_append2(&W.counters[C_MARCH0], march, at, &W.counters[C_SKIPN], skip, sat);
+        block_append2<kCameraBlock>(&W.counters[C_MARCH0], march, at, &W.counters[C_SKIPN], skip, sat);
         if (march) W.q_march[0][at] = p;
         if (skip) {
             W.q_skip[sat].origin = make_float4(rp.x, rp.y, rp.z, bitsf(p));
@@ -834,9 +836,9 @@ __global__ void __launch_bounds__(128) shade_kernel(WaveParams W, int cur) {
             W.paths[path] = R;
         }
         c_bounces += emit_march ? 1u : 0u;
-        uint32_t at = warp_append(&W.counters[C_MARCH0 + next], emit_march);
+        uint32_t at = 0, sat = 0;
+        block_append2<128>(&W.counters[C_MARCH0 + next], emit_march, at, &W.counters[C_SHADOW0 + next], emit_shadow, sat);
         if (emit_march) W.q_march[next][at] = path;
-        uint32_t sat = warp_append(&W.counters[C_SHADOW0 + next], emit_shadow);
         if (emit_shadow) W.q_shadow[next][sat] = J;
     }
     if (W.profile) {
