@@ -1058,6 +1058,14 @@ extern "C" int fpt_cuda_voxel_build_static(const struct FptRenderConfig *config,
     }
     StaticVoxelScratch *sc = g_static_scratch_addr[dev];
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The build synchronises its stream twice, which a stream capture cannot record: refuse instead of breaking
+    // the caller's graph.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (!check(cudaStreamIsCapturing(st, &capture), "cudaStreamIsCapturing", error, error_len)) return 1;
+    if (capture != cudaStreamCaptureStatusNone) {
+        set_error(error, error_len, "the allocation-free voxel build synchronises its stream and cannot run inside a stream capture");
+        return 1;
+    }
     VoxBuild B;
     for (int k = 0; k < 3; ++k) {
         B.bmin[k] = config->voxel_bounds_min[k];

@@ -739,10 +739,11 @@ int fpt_cuda_voxel_render(const struct FptRenderConfig *config,
  * brick_size 8.  Scratch lives in one fixed device array of about 2.1 MB
  * that every GPU loading the library holds until the process exits, so the
  * resolution is limited to 512.  The first call on a device looks up that
- * array's device address; make it before any stream capture.  The call
- * returns after the build has finished: it synchronises `stream` to read the
- * brick count back before the fill, and again at the end.  Every call shares
- * the array: calls that overlap on the GPU race. */
+ * array's device address; make it before any stream capture.  The call is
+ * synchronous and cannot be captured: it synchronises `stream` to read the
+ * brick count back before the fill, and again at the end, and it returns 1
+ * with an error when `stream` is capturing.  Every call shares the array:
+ * calls that overlap on the GPU race. */
 int fpt_cuda_voxel_build_static(const struct FptRenderConfig *config,
                                 const struct FptCudaSceneExt *ext,
                                 void *stream,

@@ -48,3 +48,26 @@ def test_static_build_rejects_oversize(native):
     buf = torch.zeros(16, dtype=torch.int32, device="cuda")
     with pytest.raises(native.NativeError, match="out of range"):
         native_ext.voxel_build_static(cfg, ext, buf.data_ptr(), 16, buf.data_ptr(), buf.data_ptr(), 16)
+
+
+def test_static_build_refuses_stream_capture(native):
+    """The build synchronises its stream (count readback), which a graph capture cannot hold: on a capturing
+    stream the call returns an error before it enqueues anything, and the caller's capture stays usable."""
+    torch = pytest.importorskip("torch")
+    cfg, ext = scenes.voxel_mandelbox(64, 8, 8)
+    bg = (cfg.voxel_resolution + 7) // 8
+    cap = bg ** 3 * 512
+    table = torch.zeros(bg ** 3, dtype=torch.int32, device="cuda")
+    occ = torch.zeros(cap, dtype=torch.uint8, device="cuda")
+    dist = torch.zeros(cap, dtype=torch.int16, device="cuda")
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+        with pytest.raises(native.NativeError, match="stream capture"):
+            native_ext.voxel_build_static(cfg, ext, table.data_ptr(), table.numel(), occ.data_ptr(), dist.data_ptr(), cap,
+                                          stream=side.cuda_stream)
+        table.add_(1)   # the capture still records the caller's own work
+    graph.replay()
+    torch.cuda.synchronize()
+    assert int(table.sum().item()) == table.numel()
