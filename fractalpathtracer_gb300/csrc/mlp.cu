@@ -648,7 +648,7 @@ __global__ void __launch_bounds__(128) predict_kernel(Model M, const float4 *pts
 }
 // The same prediction with the network on tcgen05: 128 points per CTA
 // iteration.  *fail_word gets bit 2 if an MMA did not complete.
-__global__ void __launch_bounds__(kTcRows) predict_tc_kernel(Model M, const float4 *pts, float *out, uint32_t n, uint32_t *fail_word) {
+__global__ void __launch_bounds__(kTcRows, 4) predict_tc_kernel(Model M, const float4 *pts, float *out, uint32_t n, uint32_t *fail_word) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TcSmem &sm = *reinterpret_cast<TcSmem *>(smem_raw);
     tc_setup(sm, M);

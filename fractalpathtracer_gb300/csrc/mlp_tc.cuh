@@ -1,11 +1,15 @@
 // mlp_tc.cuh -- the surrogate's forward pass on the 5th-generation tensor
 // cores (tcgen05): 128 rows per CTA, one row per thread.
 //
-// Per layer, one thread issues the K/16 MMAs of a 128 x 64 x K product into
-// a 128 x 64 FP32 accumulator in tensor memory and commits them to an
-// mbarrier; every thread then reads its own row of the accumulator (TMEM
-// lane = thread), adds the bias, applies SiLU and writes the BF16 row into
-// the activation tile that the next layer's MMAs read.  The arithmetic is
+// The activations live in tensor memory next to the accumulator: thread t
+// writes its row's BF16 features into TMEM lane t (two per 32-bit column),
+// and per layer one thread issues the K/16 MMAs of a 128 x 64 x K product
+// with A read from tensor memory and B (the layer's weights) from shared
+// memory, into a 128 x 64 FP32 accumulator in tensor memory, and commits
+// them to an mbarrier.  Every thread then reads its own accumulator row, adds
+// the bias, applies SiLU and writes the BF16 row back into its A lane for the
+// next layer.  Only the weights take shared memory (40 KB), so four CTAs fit
+// on an SM, each with 128 tensor-memory columns.  The arithmetic is
 // that of mlp::forward32 (BF16 features, weights and activations, FP32
 // accumulation, the f16x2-tanh SiLU of inference, FP32 output layer); only
 // the order of the FP32 sums differs.
@@ -19,6 +23,8 @@ namespace mlp {
 
 constexpr int kTcRows = 128;           // M of every MMA; the CTA has one thread per row
 constexpr uint32_t kTcCols = 64;       // tensor-memory columns: one 128 x 64 FP32 accumulator
+constexpr uint32_t kFwdCols = 128;     // a forward CTA's columns: the accumulator (0-63) and the A operand
+constexpr uint32_t kFwdA = 64;         // first column of the A operand (K / 2 columns: 56 for the features)
 constexpr uint32_t kCore = 128;        // bytes of one 8 x 8 BF16 core matrix
 // Activation tile [k chunk][row group][8 rows][8 bf16]: K-adjacent core
 // matrices lie 16 row groups apart, M-adjacent ones 128 bytes apart.
@@ -29,24 +35,23 @@ constexpr uint32_t kTcIdesc = umma::idesc_bf16_f32(kTcRows, kHid);
 constexpr unsigned long long kMmaWaitNs = 1000000000ull;   // 1 s; a layer takes about a microsecond
 
 struct TcSmem {
-    alignas(128) unsigned char act[kTcRows * kInPad * 2];    // layer-0 features (K = 112), then hidden rows (K = 64)
     alignas(128) unsigned char w0[kHid * kInPad * 2];
     alignas(128) unsigned char w[kHidden - 1][kHid * kHid * 2];
     float b[kHidden][kHid];
     float w4[kHid];
     float b4;
-    uint32_t tmem;                                          // tensor-memory base of the accumulator
+    uint32_t tmem;                                          // tensor-memory base: accumulator, then the A operand
     alignas(8) uint64_t bar;                                // MMA completion
     // Slack after the tiles: the tensor core reads each tile through a
     // descriptor, and this keeps those reads inside the CTA's shared memory
     // whatever the descriptor strides.
-    unsigned char slack[4096];
+    unsigned char slack[512];
 };
 inline size_t tc_smem_bytes() { return sizeof(TcSmem); }
 
 // Resident CTAs per SM of a kernel built on tc_forward, from its registers,
 // its shared memory, the thread and block limits and the 512 tensor-memory
-// columns.  (cudaOccupancyMaxActiveBlocksPerMultiprocessor answers 1 for
+// columns (kFwdCols per CTA).  (cudaOccupancyMaxActiveBlocksPerMultiprocessor answers 1 for
 // these kernels on GB300, where registers and shared memory allow 3.)
 inline int tc_blocks_per_sm(const void *kernel) {
     cudaFuncAttributes fa{};
@@ -60,7 +65,7 @@ inline int tc_blocks_per_sm(const void *kernel) {
     cudaDeviceGetAttribute(&blocks_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev);
     const int regs_block = ((fa.numRegs * 32 + 255) / 256) * 256 * (kTcRows / 32);   // allocated per warp in units of 256
     const int smem_block = int(tc_smem_bytes()) + int(fa.sharedSizeBytes) + smem_res;
-    int n = int(512u / kTcCols);
+    int n = int(512u / kFwdCols);
     n = regs_block > 0 ? (regs_sm / regs_block < n ? regs_sm / regs_block : n) : n;
     n = smem_sm / smem_block < n ? smem_sm / smem_block : n;
     n = threads_sm / kTcRows < n ? threads_sm / kTcRows : n;
@@ -73,8 +78,9 @@ __device__ __forceinline__ uint32_t w_core_offset(int n, int k) {
     return (uint32_t(k >> 3) * (kHid / 8) + uint32_t(n >> 3)) * kCore + uint32_t(n & 7) * 16u + uint32_t(k & 7) * 2u;
 }
 
-// Weights into the core-matrix tiles, tensor memory and the mbarrier.  All
-// threads of the 128-thread CTA call it; it ends with a barrier.
+// Weights into the core-matrix tiles, tensor memory (kFwdCols columns) and
+// the mbarrier.  All threads of the 128-thread CTA call it; it ends with a
+// barrier.
 __device__ __forceinline__ void tc_setup(TcSmem &sm, const Model &M) {
     for (int i = threadIdx.x; i < kHid * kInPad; i += blockDim.x) {
         const int n = i / kInPad, k = i - n * kInPad;
@@ -93,7 +99,7 @@ __device__ __forceinline__ void tc_setup(TcSmem &sm, const Model &M) {
     }
     if (threadIdx.x < 32) {
         __syncwarp();
-        umma::tmem_alloc(&sm.tmem, kTcCols);
+        umma::tmem_alloc(&sm.tmem, kFwdCols);
         umma::tmem_relinquish();
     }
     umma::fence_smem_to_async();   // the weight tiles are read by the tensor core
@@ -109,7 +115,7 @@ __device__ __forceinline__ void tc_teardown(TcSmem &sm) {
     if (threadIdx.x < 32) {
         __syncwarp();
         umma::fence_after_sync();
-        umma::tmem_dealloc(sm.tmem, kTcCols);
+        umma::tmem_dealloc(sm.tmem, kFwdCols);
     }
 }
 
@@ -153,18 +159,18 @@ __device__ __forceinline__ void feature_pairs(const float u[3], uint32_t f[kInPa
 // does not complete within kMmaWaitNs, every thread gets fail = true and 0.
 __device__ __forceinline__ float tc_forward(TcSmem &sm, uint32_t &phase, const float u[3], bool &fail) {
     const int t = threadIdx.x;
-    const uint32_t act = umma::smem_u32(sm.act);
+    const uint32_t lanes = uint32_t(t & ~31) << 16;   // this warp's 32 tensor-memory lanes
+    const uint32_t a_row = sm.tmem + lanes + kFwdA, d_row = sm.tmem + lanes;
     {
         uint32_t f[kInPad / 2];
         feature_pairs(u, f);
 #pragma unroll
-        for (int kc = 0; kc < kInPad / 8; ++kc) umma::st_shared_v4(act + act_offset(t, kc), f[4 * kc], f[4 * kc + 1], f[4 * kc + 2], f[4 * kc + 3]);
+        for (int q = 0; q < kInPad / 16; ++q) umma::tmem_st8(a_row + 8u * uint32_t(q), f + 8 * q);
+        umma::tmem_wait_st();
     }
-    const uint32_t row_taddr = sm.tmem + (uint32_t(t & ~31) << 16);   // this warp's 32 lanes
     float out = 0.0f;
 #pragma unroll 1
     for (int L = 0; L < kHidden; ++L) {
-        umma::fence_smem_to_async();
         umma::fence_before_sync();
         __syncthreads();
         if (t == 0) {
@@ -172,8 +178,8 @@ __device__ __forceinline__ float tc_forward(TcSmem &sm, uint32_t &phase, const f
             const int ksteps = (L == 0 ? kInPad : kHid) / 16;
             const uint32_t b = umma::smem_u32(L == 0 ? sm.w0 : sm.w[L - 1]);
             for (int j = 0; j < ksteps; ++j)
-                umma::mma_bf16(sm.tmem, umma::smem_desc(act + uint32_t(j) * 2u * kActK, kActK, kCore),
-                               umma::smem_desc(b + uint32_t(j) * 2u * kWK, kWK, kCore), kTcIdesc, uint32_t(j));
+                umma::mma_bf16_ts(sm.tmem, sm.tmem + kFwdA + 8u * uint32_t(j), umma::smem_desc(b + uint32_t(j) * 2u * kWK, kWK, kCore),
+                                  kTcIdesc, uint32_t(j));
             umma::mma_commit(&sm.bar);
         }
         const int late = t == 0 ? int(!umma::mbar_wait(&sm.bar, phase, kMmaWaitNs)) : 0;
@@ -184,29 +190,32 @@ __device__ __forceinline__ float tc_forward(TcSmem &sm, uint32_t &phase, const f
         }
         umma::fence_after_sync();
         __syncwarp();
-        uint32_t r[64];
-        umma::tmem_ld64(row_taddr, r);
         const float *bias = sm.b[L];
-        if (L + 1 < kHidden) {
 #pragma unroll
-            for (int kc = 0; kc < kHid / 8; ++kc) {
-                uint32_t h[4];
+        for (int h = 0; h < 2; ++h) {   // the accumulator row in two halves of 32 columns
+            uint32_t r[32];
+            umma::tmem_ld32(d_row + 32u * uint32_t(h), r);
+            if (L + 1 < kHidden) {
+                uint32_t a[16];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int c = kc * 8 + q * 2;
-                    h[q] = silu2_bf16(__uint_as_float(r[c]) + bias[c], __uint_as_float(r[c + 1]) + bias[c + 1]);
+                for (int q = 0; q < 16; ++q) {
+                    const int c = h * 32 + q * 2;
+                    a[q] = silu2_bf16(__uint_as_float(r[2 * q]) + bias[c], __uint_as_float(r[2 * q + 1]) + bias[c + 1]);
                 }
-                umma::st_shared_v4(act + act_offset(t, kc), h[0], h[1], h[2], h[3]);
-            }
-        } else {
-            // Output layer: dot product of the (bf16-rounded) last activations with W4.
+                umma::tmem_st8(a_row + 16u * uint32_t(h), a);
+                umma::tmem_st8(a_row + 16u * uint32_t(h) + 8u, a + 8);
+            } else {
+                // Output layer: dot product of the (bf16-rounded) last activations with W4.
 #pragma unroll
-            for (int c = 0; c < kHid; c += 2) {
-                const uint32_t h = silu2_bf16(__uint_as_float(r[c]) + bias[c], __uint_as_float(r[c + 1]) + bias[c + 1]);
-                out += __uint_as_float(h << 16) * sm.w4[c] + __uint_as_float(h & 0xffff0000u) * sm.w4[c + 1];
+                for (int q = 0; q < 16; ++q) {
+                    const int c = h * 32 + q * 2;
+                    const uint32_t hh = silu2_bf16(__uint_as_float(r[2 * q]) + bias[c], __uint_as_float(r[2 * q + 1]) + bias[c + 1]);
+                    out += __uint_as_float(hh << 16) * sm.w4[c] + __uint_as_float(hh & 0xffff0000u) * sm.w4[c + 1];
+                }
             }
-            out += sm.b4;
         }
+        if (L + 1 < kHidden) umma::tmem_wait_st();
+        else out += sm.b4;
     }
     return out;
 }

@@ -355,7 +355,7 @@ __device__ __forceinline__ uint32_t feed_take(SkipFeed &F, bool need, const Wave
 // 128-thread CTA proposes runs one 128-row forward pass (mlp::tc_forward).
 // Guard word bits: 1 = loop time limit, 2 = an MMA did not complete.
 template <int KIND>
-__global__ void __launch_bounds__(mlp::kTcRows, 3) skip_march_tc_kernel(WaveParams W, SkipArgs A) {
+__global__ void __launch_bounds__(mlp::kTcRows, 4) skip_march_tc_kernel(WaveParams W, SkipArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
     const DeviceScene &S = c_scene;
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(32 * kSkipWarps, 3) skip_primary_kernel(const 
 // skip_primary_kernel with the network on tcgen05: 128 pixels per CTA
 // iteration, CTA-synchronous skip loop.
 template <int KIND>
-__global__ void __launch_bounds__(mlp::kTcRows, 3) skip_primary_tc_kernel(const DeviceScene *scene, SkipArgs A,
+__global__ void __launch_bounds__(mlp::kTcRows, 4) skip_primary_tc_kernel(const DeviceScene *scene, SkipArgs A,
                                                                           FptCudaPrimaryHit *hits) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     mlp::TcSmem &sm = *reinterpret_cast<mlp::TcSmem *>(smem_raw);
