@@ -232,16 +232,19 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-// SiLU of two values for inference: sigmoid from one packed f16x2 tanh
-// (half the MUFU work of two f32 tanh), product and rounding in f32.
-__device__ __forceinline__ uint32_t silu2_bf16(float z0, float z1) {
-    const __half2 hz = __floats2half2_rn(0.5f * z0, 0.5f * z1);
-    uint32_t t, s;
-    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const uint32_t *>(&hz)));
-    asm("fma.rn.f16x2 %0, %1, %2, %2;" : "=r"(s) : "r"(t), "r"(0x38003800u));   // 0.5 t + 0.5
-    const float2 sf = __half22float2(*reinterpret_cast<const __half2 *>(&s));
-    return pack_bf16(z0 * sf.x, z1 * sf.y);
+// SiLU of two values for inference, from their halves h = z / 2:
+// z sigmoid(z) = h + h tanh(h), with the tanh from one packed f16x2 MUFU op
+// (half the MUFU work of two f32 tanh) and h, the product and the rounding
+// to BF16 in f32.  A caller that adds a bias first can pass
+// fmaf(z, 0.5, b / 2), which equals (z + b) / 2 exactly.
+__device__ __forceinline__ uint32_t silu2_bf16_half(float h0, float h1) {
+    const __half2 hh = __floats2half2_rn(h0, h1);
+    uint32_t t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const uint32_t *>(&hh)));
+    const float2 tf = __half22float2(*reinterpret_cast<const __half2 *>(&t));
+    return pack_bf16(fmaf(h0, tf.x, h0), fmaf(h1, tf.y, h1));
 }
+__device__ __forceinline__ uint32_t silu2_bf16(float z0, float z1) { return silu2_bf16_half(0.5f * z0, 0.5f * z1); }
 
 // SiLU epilogue that turns the accumulators of a 32 x 64 layer output (two
 // m16 tiles x eight n8 tiles) into the A fragments of the next layer's

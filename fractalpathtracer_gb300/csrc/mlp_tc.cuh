@@ -37,7 +37,7 @@ constexpr unsigned long long kMmaWaitNs = 1000000000ull;   // 1 s; a layer takes
 struct TcSmem {
     alignas(128) unsigned char w0[kHid * kInPad * 2];
     alignas(128) unsigned char w[kHidden - 1][kHid * kHid * 2];
-    float b[kHidden][kHid];
+    float b[kHidden][kHid];                                 // half biases, b / 2 (silu2_bf16_half)
     float w4[kHid];
     float b4;
     uint32_t tmem;                                          // tensor-memory base: accumulator, then the A operand
@@ -91,7 +91,7 @@ __device__ __forceinline__ void tc_setup(TcSmem &sm, const Model &M) {
             const int n = i / kHid, k = i - n * kHid;
             *reinterpret_cast<__nv_bfloat16 *>(sm.w[l - 1] + w_core_offset(n, k)) = M.wbf[w_offset(l) + i];
         }
-    for (int i = threadIdx.x; i < kHidden * kHid; i += blockDim.x) sm.b[i / kHid][i % kHid] = M.params[b_offset(i / kHid) + i % kHid];
+    for (int i = threadIdx.x; i < kHidden * kHid; i += blockDim.x) sm.b[i / kHid][i % kHid] = 0.5f * M.params[b_offset(i / kHid) + i % kHid];
     for (int i = threadIdx.x; i < kHid; i += blockDim.x) sm.w4[i] = __bfloat162float(M.wbf[kW4 + i]);
     if (threadIdx.x == 0) {
         sm.b4 = M.params[kB4];
@@ -200,7 +200,7 @@ __device__ __forceinline__ float tc_forward(TcSmem &sm, uint32_t &phase, const f
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     const int c = h * 32 + q * 2;
-                    a[q] = silu2_bf16(__uint_as_float(r[2 * q]) + bias[c], __uint_as_float(r[2 * q + 1]) + bias[c + 1]);
+                    a[q] = silu2_bf16_half(fmaf(__uint_as_float(r[2 * q]), 0.5f, bias[c]), fmaf(__uint_as_float(r[2 * q + 1]), 0.5f, bias[c + 1]));
                 }
                 umma::tmem_st8(a_row + 16u * uint32_t(h), a);
                 umma::tmem_st8(a_row + 16u * uint32_t(h) + 8u, a + 8);
@@ -209,7 +209,8 @@ __device__ __forceinline__ float tc_forward(TcSmem &sm, uint32_t &phase, const f
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     const int c = h * 32 + q * 2;
-                    const uint32_t hh = silu2_bf16(__uint_as_float(r[2 * q]) + bias[c], __uint_as_float(r[2 * q + 1]) + bias[c + 1]);
+                    const uint32_t hh =
+                        silu2_bf16_half(fmaf(__uint_as_float(r[2 * q]), 0.5f, bias[c]), fmaf(__uint_as_float(r[2 * q + 1]), 0.5f, bias[c + 1]));
                     out += __uint_as_float(hh << 16) * sm.w4[c] + __uint_as_float(hh & 0xffff0000u) * sm.w4[c + 1];
                 }
             }
