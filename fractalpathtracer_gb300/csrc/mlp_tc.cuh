@@ -51,8 +51,9 @@ inline size_t tc_smem_bytes() { return sizeof(TcSmem); }
 
 // Resident CTAs per SM of a kernel built on tc_forward, from its registers,
 // its shared memory, the thread and block limits and the 512 tensor-memory
-// columns (kFwdCols per CTA).  (cudaOccupancyMaxActiveBlocksPerMultiprocessor answers 1 for
-// these kernels on GB300, where registers and shared memory allow 3.)
+// columns (kFwdCols per CTA).  (cudaOccupancyMaxActiveBlocksPerMultiprocessor
+// answers 1 for these kernels on GB300, where registers, shared memory and
+// tensor memory allow 4.)
 inline int tc_blocks_per_sm(const void *kernel) {
     cudaFuncAttributes fa{};
     int dev = 0;
