@@ -183,7 +183,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
-    ap.add_argument("--only", default="", choices=["", "plain", "box", "skip", "voxel", "train"],
+    ap.add_argument("--only", default="", choices=["", "plain", "box", "skip", "voxel", "train", "predict"],
                     help="render only this march (profiling runs: no training unless skip, no JSON contract line)")
     ap.add_argument("--res", default=f"{W}x{H}", help="--only runs: image size WxH")
     ap.add_argument("--spp", type=int, default=SPP, help="--only runs: samples per pixel")
@@ -502,6 +502,24 @@ def run_only(args):
         model, st = nx.mlp_create(b.cfg, b.ext, mc)
         nx.mlp_destroy(model)
         print(json.dumps({"only": "train", "steps": mc.steps, "train_ms": st["train_ms"], "loss_last": st["loss_last"]}), flush=True)
+        return
+    if args.only == "predict":   # the network alone: 8M-row predictions with seeded parameters (host copies included)
+        b = scenes.mandelbulb_path(64, 64, 1)
+        lo, hi = scenes.SURROGATE_BOXES["mandelbulb"]
+        model, _ = nx.mlp_create(b.cfg, b.ext, nx.mlp_config(lo, hi, points=1 << 16, steps=1, batch=4096, seed=1))
+        nx.mlp_set_params(model, scenes.random_mlp_params(11))
+        rng = np.random.default_rng(5)
+        pts = np.zeros((1 << 23, 4), np.float32)
+        pts[:, :3] = rng.uniform(-1.25, 1.25, (1 << 23, 3))
+        for _ in range(args.warmup):
+            nx.mlp_predict(model, pts)
+        ms = []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            nx.mlp_predict(model, pts)
+            ms.append((time.perf_counter() - t) * 1e3)
+        nx.mlp_destroy(model)
+        print(json.dumps({"only": "predict", "engine": args.engine, "rows": len(pts), "ms_with_copies": ms}), flush=True)
         return
     if args.only == "voxel":   # Mandelbox occupancy bricks (1024^3 by default), primary + shadow DDA
         cfg, ext = scenes.voxel_mandelbox(args.voxel_res, w, h)
