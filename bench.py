@@ -224,22 +224,29 @@ def main():
             torch.cuda.synchronize()
 
     def series(e, steps, clocks=None):
-        """Device-timed renders (library CUDA events) with L2 flushed before each; per-kernel spans recorded."""
+        """Device-timed renders (library CUDA events) with L2 flushed before each.  The timed renders carry no
+        profile counters (their atomics would add work to the kernels), only per-kernel event spans; the
+        evaluation counts come from one profile render after them (the same frame, the same counts)."""
         out = {"ms": [], "march_ms": 0.0, "march_launches": 0, "march_evals": 0, "skip_ms": 0.0, "shade_ms": 0.0,
                "launches": 0, "phase_evals": None}
-        for _ in range(steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            _, _, ms, prof = native.cuda_render(cfg, e, linear=False, profile=True)
-            rs = nx.render_stats()
-            out["ms"].append(ms)
-            out["march_ms"] += rs["march_ms"]
-            out["march_launches"] += rs["march_launches"]
-            out["march_evals"] += rs["march_evals"]
-            out["skip_ms"] += rs["skip_ms"]
-            out["shade_ms"] += rs["shade_ms"]
-            out["launches"] += rs["kernel_launches"]
-            out["phase_evals"] = [int(prof.primary_steps), int(prof.secondary_steps), int(prof.shadow_steps)]
+        nx.set_kernel_timing(True)
+        try:
+            for _ in range(steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                _, _, ms = native.cuda_render(cfg, e, linear=False)
+                rs = nx.render_stats()
+                out["ms"].append(ms)
+                out["march_ms"] += rs["march_ms"]
+                out["march_launches"] += rs["march_launches"]
+                out["skip_ms"] += rs["skip_ms"]
+                out["shade_ms"] += rs["shade_ms"]
+                out["launches"] += rs["kernel_launches"]
+        finally:
+            nx.set_kernel_timing(False)
+        _, _, _, prof = native.cuda_render(cfg, e, linear=False, profile=True)
+        out["march_evals"] = nx.render_stats()["march_evals"] * steps
+        out["phase_evals"] = [int(prof.primary_steps), int(prof.secondary_steps), int(prof.shadow_steps)]
         return out
 
     # End-to-end through the public call: the results land in pinned host buffers (allocated once, reused).

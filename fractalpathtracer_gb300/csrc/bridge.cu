@@ -479,7 +479,7 @@ int render_core(const FptRenderConfig *config, const FptCudaSceneExt *ext, const
     pl.launches = &launches;
     uint32_t grids[2] = {0, 0};
     pl.grids = grids;
-    if (want_profile) {
+    if (want_profile || c.kernel_timing) {   // per-kernel spans: profile renders, or any render with kernel timing on
         if (!c.timer_events) {
             c.timer_capacity = 1024;
             c.timer_events = new cudaEvent_t[c.timer_capacity];
@@ -1044,6 +1044,13 @@ int fpt_cuda_set_march_schedule(uint32_t schedule, uint32_t batch) {
 int fpt_cuda_set_loop_limit(uint64_t limit_ns) {
     std::lock_guard<std::mutex> lock(ctx().mutex);
     ctx().loop_limit_ns = limit_ns;
+    return 0;
+}
+
+int fpt_cuda_set_kernel_timing(uint32_t on) {
+    if (on > 1u) return 1;
+    std::lock_guard<std::mutex> lock(ctx().mutex);
+    ctx().kernel_timing = on;
     return 0;
 }
 

@@ -40,6 +40,7 @@ struct Context {
     uint32_t refill_batch = 0;
     unsigned long long loop_limit_ns = 0;   // persistent-loop time limit of later renders (0: 10 s)
     uint32_t network_engine = 0;   // FPT_CUDA_NET_*: surrogate network on tcgen05 (0) or mma.sync (1)
+    uint32_t kernel_timing = 0;    // per-kernel event spans in renders without profile statistics too
 };
 
 Context &ctx();

@@ -27,6 +27,7 @@ EXPORTED = [
     "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch", "fpt_cuda_set_launch_shape",
     "fpt_cuda_set_march_schedule",
     "fpt_cuda_set_network_engine",
+    "fpt_cuda_set_kernel_timing",
     "fpt_test_bounded_waits",
     "fpt_cuda_set_loop_limit",
     "fpt_cuda_set_device", "fpt_cuda_get_device", "fpt_cuda_hdri_lut",

@@ -89,6 +89,7 @@ def declare(L: C.CDLL) -> None:
     L.fpt_cuda_set_launch_shape.argtypes = [C.c_uint32, C.c_int32]
     L.fpt_cuda_set_march_schedule.argtypes = [C.c_uint32, C.c_uint32]
     L.fpt_cuda_set_network_engine.argtypes = [C.c_uint32]
+    L.fpt_cuda_set_kernel_timing.argtypes = [C.c_uint32]
     L.fpt_test_bounded_waits.argtypes = [P(C.c_uint32), C.c_size_t] + err
     L.fpt_cuda_set_loop_limit.argtypes = [C.c_uint64]
     L.fpt_cuda_render_batch.argtypes = [cfg, ext, C.c_size_t, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_size_t,
@@ -98,8 +99,8 @@ def declare(L: C.CDLL) -> None:
                  "fpt_cuda_voxel_build_static", "fpt_cuda_mlp_create", "fpt_cuda_mlp_destroy", "fpt_cuda_mlp_predict",
                  "fpt_cuda_mlp_get_params", "fpt_cuda_mlp_set_params", "fpt_cuda_mlp_gradients", "fpt_cuda_skip_stats",
                  "fpt_cuda_render_stats", "fpt_cuda_render_batch", "fpt_cuda_autotune_batch", "fpt_cuda_set_launch_shape",
-                 "fpt_cuda_set_march_schedule", "fpt_cuda_set_network_engine", "fpt_test_bounded_waits",
-                 "fpt_cuda_set_loop_limit"):
+                 "fpt_cuda_set_march_schedule", "fpt_cuda_set_network_engine", "fpt_cuda_set_kernel_timing",
+                 "fpt_test_bounded_waits", "fpt_cuda_set_loop_limit"):
         getattr(L, name).restype = C.c_int
 
 
@@ -337,6 +338,13 @@ def set_network_engine(engine: int = NET_TCGEN05) -> None:
     from .native import lib
     if lib().fpt_cuda_set_network_engine(engine) != 0:
         raise ValueError("engine must be NET_TCGEN05 (0) or NET_MMA_SYNC (1)")
+
+
+def set_kernel_timing(on: bool = True) -> None:
+    """Per-kernel event spans (render_stats march/shade/skip ms) in every later render, not only profile renders."""
+    from .native import lib
+    if lib().fpt_cuda_set_kernel_timing(1 if on else 0) != 0:
+        raise ValueError("kernel timing is on (1) or off (0)")
 
 
 def set_march_schedule(schedule: int = 0, batch: int = 0) -> None:

@@ -836,8 +836,9 @@ int fpt_test_bounded_waits(uint32_t *result, size_t result_len, char *error, siz
 
 /* Launch and timing record of the last fpt_cuda_render / fpt_metal_render
  * (no counterpart in the reference).  Kernel times are sums of CUDA-event
- * spans on the library's stream around each launch; they are recorded only
- * when the call asked for profile statistics. */
+ * spans on the library's stream around each launch; they are recorded when
+ * the call asked for profile statistics or kernel timing is on
+ * (fpt_cuda_set_kernel_timing).  Evaluation counts need profile statistics. */
 struct FptCudaRenderStats {
     uint64_t kernel_launches;    /* kernels launched by the render */
     uint64_t march_launches;
@@ -853,6 +854,12 @@ struct FptCudaRenderStats {
     uint32_t skip_grid;          /* blocks of the persistent skip kernel (0: no skip pass) */
 };
 int fpt_cuda_render_stats(struct FptCudaRenderStats *stats);
+
+/* Kernel timing of later renders (no counterpart in the reference): 1 records
+ * the per-kernel event spans of FptCudaRenderStats in every render, without
+ * the profile counters (whose atomics add work to the kernels); 0 (default)
+ * records them only in profile renders.  Returns 1 for other values. */
+int fpt_cuda_set_kernel_timing(uint32_t on);
 
 /* Launch shape of later single-scene renders (no counterpart in the
  * reference): paths per wave (0: min(all paths of a launch, 64M)) and the
