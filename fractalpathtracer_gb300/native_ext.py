@@ -343,7 +343,7 @@ def set_network_engine(engine: int = NET_TCGEN05) -> None:
 def set_kernel_timing(on: bool = True) -> None:
     """Per-kernel event spans (render_stats march/shade/skip ms) in every later render, not only profile renders."""
     from .native import lib
-    if lib().fpt_cuda_set_kernel_timing(1 if on else 0) != 0:
+    if lib().fpt_cuda_set_kernel_timing(int(on)) != 0:
         raise ValueError("kernel timing is on (1) or off (0)")
 
 

@@ -109,6 +109,9 @@ def test_settings_validate_arguments_without_gpu(native):
         nx.set_march_schedule(1, 0)
     with pytest.raises(ValueError):
         nx.set_march_schedule(0, 33)
+    with pytest.raises(ValueError):
+        nx.set_kernel_timing(2)
+    nx.set_kernel_timing(False)
     nx.set_network_engine(nx.NET_MMA_SYNC)
     nx.set_network_engine(nx.NET_TCGEN05)
     nx.set_march_schedule(0, 0)

@@ -165,6 +165,24 @@ def test_profile_stats(native):
     assert abs(est - ms) <= 1e-6 * ms + 1e-9
 
 
+def test_kernel_timing_without_profile(native):
+    """fpt_cuda_set_kernel_timing: per-kernel event spans in a render without profile counters (the bench's timed
+    renders); without it only profile renders record them.  The image does not change."""
+    from fractalpathtracer_gb300 import native_ext as nx
+    b = scenes.mandelbulb_path(160, 90, 2)
+    _, plain, _ = native.cuda_render(b.cfg, b.ext, linear=False)
+    assert nx.render_stats()["march_ms"] == 0.0
+    nx.set_kernel_timing(True)
+    try:
+        _, timed, _ = native.cuda_render(b.cfg, b.ext, linear=False)
+        rs = nx.render_stats()
+    finally:
+        nx.set_kernel_timing(False)
+    assert rs["march_launches"] == b.cfg.render[0] + 1 and rs["march_ms"] > 0.0 and rs["shade_ms"] > 0.0
+    assert rs["march_evals"] == 0   # counts need profile statistics
+    assert np.array_equal(plain, timed)
+
+
 def test_loop_time_limit(native):
     """A persistent loop that reaches its time limit stops and the render reports it (no fault); with the default
     limit back, the next render is the same as before."""
