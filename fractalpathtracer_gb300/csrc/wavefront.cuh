@@ -7,8 +7,9 @@
 //   camera_kernel   writes every path's camera ray into the march queue
 //   march_kernel    persistent: each lane takes one march job (a path ray or
 //                   a sun shadow ray) from the queue, marches it with one
-//                   distance evaluation per loop iteration, and on finishing
-//                   takes the next job at once (per-lane regeneration, one
+//                   distance evaluation per loop iteration, and once it has
+//                   finished takes the next job together with the warp's
+//                   other finished lanes (per-lane regeneration in groups, one
 //                   warp-aggregated atomic per refill); hits go to the shade
 //                   queue, misses add the environment
 //   shade_kernel    material, normal, sun shadow ray, scatter and Russian
