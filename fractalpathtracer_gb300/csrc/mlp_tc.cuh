@@ -123,15 +123,12 @@ __device__ __forceinline__ void tc_teardown(TcSmem &sm) {
 // The features of mlp::features, as 56 packed BF16 pairs (element 2p in the
 // low half of pair p).
 __device__ __forceinline__ void feature_pairs(const float u[3], uint32_t f[kInPad / 2]) {
+    float v[kInPad];   // the features in input order (the compiler keeps only the pending ones live)
 #pragma unroll
-    for (int p = 0; p < kInPad / 2; ++p) f[p] = 0u;
-    auto put = [&](int e, float v) {
-        const uint32_t b = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v)));
-        f[e >> 1] |= (e & 1) ? (b << 16) : b;
-    };
-    put(0, u[0]);
-    put(1, u[1]);
-    put(2, u[2]);
+    for (int e = kIn; e < kInPad; ++e) v[e] = 0.0f;
+    v[0] = u[0];
+    v[1] = u[1];
+    v[2] = u[2];
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
         const float fr = 3.14159265358979f * exp2f(0.4f * float(r));
@@ -141,8 +138,8 @@ __device__ __forceinline__ void feature_pairs(const float u[3], uint32_t f[kInPa
             __sincosf(fr * u[i], &s, &c);
 #pragma unroll
             for (int k = r; k < kFreq; k += 5) {
-                put(3 + (k * 3 + i) * 2, s);
-                put(3 + (k * 3 + i) * 2 + 1, c);
+                v[3 + (k * 3 + i) * 2] = s;
+                v[3 + (k * 3 + i) * 2 + 1] = c;
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {   // angle x 4
                     float s2 = 2.0f * s * c, c2 = 1.0f - 2.0f * s * s;
@@ -152,6 +149,8 @@ __device__ __forceinline__ void feature_pairs(const float u[3], uint32_t f[kInPa
             }
         }
     }
+#pragma unroll
+    for (int p = 0; p < kInPad / 2; ++p) f[p] = pack_bf16(v[2 * p], v[2 * p + 1]);   // one conversion per pair
 }
 
 // Forward pass of the CTA's 128 rows: every thread passes its row's
